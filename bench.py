@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""bench.py -- PageRank throughput of libgtc on one GB300.
+
+Workload (default ``rmat24``): the 268M-draw R-MAT graph -- scale 24
+(16,777,216 vertices), edge factor 16, (a,b,c,d) = (0.57,0.19,0.19,0.05),
+vertex ids randomly relabelled, duplicate edges removed (first draw kept,
+draw order kept), self-loops kept -- generated on the GPU from a fixed seed.
+Unweighted PageRank, uniform personalisation, damping 0.85, epsilon 1e-7
+(L1 change per sweep), FP32 vectors with FP64 reductions.
+
+A step is one complete PageRank solve (pagerank, centrality.rs:234-248 of
+graph-tool-rs) from the uniform start to convergence.  The metric is GTEPS =
+edges x sweeps / seconds / 1e9.
+
+  value     device-resident: gtc_pagerank_device on a CUDA tensor, CUDA
+            events around K steps on the library's stream.
+  e2e       the reference-facing C ABI call gtc_pagerank with host FP64
+            buffers: the warm-start map (8n bytes) goes in and the result
+            (8n bytes) comes back every step, from pinned memory.
+  roofline  the sweep kernel: algorithmic bytes per sweep (below) over its
+            CUDA-event duration (gtc_options.timing), against the measured
+            HBM copy bandwidth.
+            B = 4(n+1) + 4m + 4mW + 4n (gather) + 4n (prev) + 4n (next)
+                + 4n (y = next/deg) + 4nP          (W = weighted, P = pers)
+  cpu_baseline  the CPU oracle (a C restatement of the reference's f64
+            path, all host threads) on the same graph, bounded to a few sweeps.
+
+``--impl reference`` times that CPU restatement alone (the reference itself
+is Rust and cannot be built here).  Inputs are larger than L2 (the graph's
+index arrays alone are ~1 GB), so no flush runs between steps.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "graph-tool-rs_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+WORKLOADS = {
+    "rmat24": dict(gen="rmat", scale=24, edge_factor=16, seed=1, weighted=False, eps=1e-7,
+                   label="R-MAT scale 24, edge factor 16 (268,435,456 draws), "
+                         "(0.57,0.19,0.19,0.05), relabelled, deduplicated, unweighted"),
+    "rmat24w": dict(gen="rmat", scale=24, edge_factor=16, seed=1, weighted=True, eps=1e-7,
+                    label="R-MAT scale 24, edge factor 16, FP32 weights U(0.1,1)"),
+    "chunglu": dict(gen="chunglu", n=4_194_304, m=67_108_864, seed=2, weighted=True, eps=1e-7,
+                    label="Chung-Lu n=4,194,304 m~67M, Pareto(2.1, min 2, cap 1e5) "
+                          "degrees, FP32 weights U(0.1,1), weighted"),
+    "rmat20": dict(gen="rmat", scale=20, edge_factor=16, seed=1, weighted=False, eps=1e-7,
+                   label="R-MAT scale 20, edge factor 16 (small test size)"),
+}
+DAMPING = 0.85
+MAX_ITER = 1000  # a safety cap; the solves converge far below it
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_graph(wl, device, rank):
+    import torch
+    from graph_tool import synth_gpu
+    if wl["gen"] == "rmat":
+        n, src, tgt = synth_gpu.rmat(wl["scale"], wl["edge_factor"], seed=wl["seed"] + rank,
+                                     device=device)
+        w = None
+        if wl["weighted"]:
+            u = synth_gpu._unit(synth_gpu.splitmix(wl["seed"] + 1000, 0, src.numel(), device))
+            w = (0.1 + 0.9 * u).to(torch.float32)
+    else:
+        n, src, tgt, w = synth_gpu.chung_lu(wl["n"], wl["m"], seed=wl["seed"] + rank,
+                                            device=device)
+    torch.cuda.synchronize()
+    return n, src.contiguous(), tgt.contiguous(), w
+
+
+def algorithmic_bytes(n, m, weighted, pers=False):
+    return 4 * (n + 1) + 4 * m + (4 * m if weighted else 0) + 16 * n + (4 * n if pers else 0)
+
+
+def cpu_sample(n, src_np, tgt_np, w_np, eps, sweeps, threads):
+    """The CPU oracle on the same graph, bounded to `sweeps` sweeps."""
+    import oracle as O
+    O.build()
+    t0 = time.perf_counter()
+    g = O.Graph(n)
+    g.add_edge_arrays(src_np, tgt_np)
+    build_s = time.perf_counter() - t0
+    return g, build_s
+
+
+def run_cpu(g, m, w_np, eps, sweeps, threads):
+    t0 = time.perf_counter()
+    _, it = g.pagerank(weight=w_np, damping=DAMPING, epsilon=eps, max_iter=sweeps, grain=4096,
+                       threads=threads)
+    dt = time.perf_counter() - t0
+    return m * it / dt / 1e9, dt, it
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gtc", choices=["gtc", "reference"])
+    ap.add_argument("--workload", default="rmat24", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-sweeps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    rank, world, local = env_rank()
+
+    import numpy as np
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference" and rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    n, src, tgt, w = make_graph(wl, device, rank)
+    m = int(src.numel())
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        import oracle as O
+        src_np = src.cpu().numpy().astype(np.uint32)
+        tgt_np = tgt.cpu().numpy().astype(np.uint32)
+        w_np = None if w is None else w.cpu().double().numpy()
+        del src, tgt, w
+        torch.cuda.empty_cache()
+        g, build_s = cpu_sample(n, src_np, tgt_np, w_np, wl["eps"], args.cpu_sweeps, threads)
+        for _ in range(args.warmup):
+            run_cpu(g, m, w_np, wl["eps"], args.cpu_sweeps, threads)
+        tot_t, tot_it = 0.0, 0
+        for _ in range(args.steps):
+            _, dt, it = run_cpu(g, m, w_np, wl["eps"], args.cpu_sweeps, threads)
+            tot_t += dt
+            tot_it += it
+        v = m * tot_it / tot_t / 1e9
+        sample = (f"{args.cpu_sweeps} sweeps of the full {args.workload} graph per step "
+                  f"(n={n}, m={m}), gtc_oracle.c pagerank with {threads} OpenMP threads")
+        print(json.dumps({
+            "impl": "reference", "metric": "PageRank GTEPS", "value": v, "unit": "GTEPS",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "graph": wl["label"], "n": n, "m": m,
+                       "damping": DAMPING, "epsilon": wl["eps"]},
+            "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference is Rust (graph-tool-rs); no Rust toolchain exists on this "
+                    "machine, so its CPU path is timed through the C restatement in oracle/",
+        }), flush=True)
+        return
+
+    from graph_tool import _ffi
+    L = _ffi.lib()
+    stream = torch.cuda.current_stream(device)
+    h = C.c_void_p()
+    _ffi.check(L.gtc_graph_create_device(n, m, C.c_void_p(src.data_ptr()),
+                                         C.c_void_p(tgt.data_ptr()),
+                                         C.c_void_p(stream.cuda_stream), C.byref(h)))
+    _ffi.check(L.gtc_graph_set_stream(h, C.c_void_p(stream.cuda_stream)))
+    wvec = _ffi.DVec.of(w) if w is not None else None
+    params = _ffi.PowerIteration(wl["eps"], MAX_ITER, n, (n + 4095) // 4096)
+    rank_t = torch.empty(n, dtype=torch.float32, device=device)
+    rvec = _ffi.DVec.of(rank_t)
+    opt = _ffi.Options(_ffi.GTC_PREC_F32, 0, C.c_void_p(stream.cuda_stream), 1, 0)
+
+    def solve_device():
+        res = _ffi.Result()
+        _ffi.check(L.gtc_pagerank_device(h, None, C.byref(wvec) if wvec else None, None,
+                                         DAMPING, C.byref(params), C.byref(rvec), 0,
+                                         C.byref(opt), C.byref(res)))
+        return res
+
+    for _ in range(args.warmup):
+        solve_device()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    sweeps = sweep_ms = launches = sweep_launches = 0
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            r = solve_device()
+            sweeps += r.iterations
+            sweep_ms += r.sweep_ms
+            launches += r.launches
+            sweep_launches += r.sweep_launches
+        e1.record(stream)
+        torch.cuda.synchronize()
+    t_ms = e0.elapsed_time(e1)
+    if world > 1:
+        tt = torch.tensor([t_ms], dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    value = world * m * sweeps / (t_ms / 1e3) / 1e9
+    iters_per_solve = sweeps / args.steps
+
+    # ---- e2e through the host-buffer C ABI ------------------------------
+    w_host = None
+    if w is not None:
+        w_host = torch.empty(m, dtype=torch.float64, pin_memory=True)
+        w_host.copy_(w.double())
+    rank_host = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    rank_np = rank_host.numpy()
+    w_np = None if w_host is None else w_host.numpy()
+    e2e_params = _ffi.PowerIteration(wl["eps"], MAX_ITER, n, (n + 4095) // 4096)
+    opt_h = _ffi.Options(_ffi.GTC_PREC_F32, 0, C.c_void_p(stream.cuda_stream), 0, 0)
+
+    def solve_host():
+        rank_np[:] = 1.0 / n  # the warm-start map the caller hands in
+        res = _ffi.Result()
+        _ffi.check(L.gtc_pagerank(h, None, _ffi.ptr(w_np, _ffi.f64p), 0 if w_np is None else m,
+                                  None, 0, DAMPING, C.byref(e2e_params),
+                                  _ffi.ptr(rank_np, _ffi.f64p), n, n, C.byref(opt_h),
+                                  C.byref(res)))
+        return res
+
+    solve_host()
+    torch.cuda.synchronize()
+    e2e_sweeps = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_sweeps += solve_host().iterations
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": world * m * e2e_sweeps / e2e_s / 1e9, "unit": "GTEPS",
+           "h2d_bytes_per_step": 8 * n + (8 * m if w is not None else 0),
+           "d2h_bytes_per_step": 8 * n,
+           "ms_per_step": 1e3 * e2e_s / args.steps}
+
+    # ---- roofline of the sweep kernel ------------------------------------
+    peak, peak_kind = measured_peaks()
+    bytes_per_sweep = algorithmic_bytes(n, m, w is not None)
+    sweep_avg_s = (sweep_ms / 1e3) / max(sweeps, 1)
+    achieved = bytes_per_sweep / sweep_avg_s / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
+    if os.path.exists(prof):
+        traffic = json.load(open(prof)).get("bytes_per_launch")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                "kernel": "k_pr_f32 sweep", "bytes_per_launch": bytes_per_sweep,
+                "avg_launch_us": sweep_avg_s * 1e6}
+
+    # ---- CPU baseline ------------------------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        src_np = src.cpu().numpy().astype(np.uint32)
+        tgt_np = tgt.cpu().numpy().astype(np.uint32)
+        w_cpu = None if w is None else w.cpu().double().numpy()
+        g, build_s = cpu_sample(n, src_np, tgt_np, w_cpu, wl["eps"], args.cpu_sweeps, threads)
+        v, dt, it = run_cpu(g, m, w_cpu, wl["eps"], args.cpu_sweeps, threads)
+        cpu = {"value": v, "unit": "GTEPS", "cores": threads, "kind": "port",
+               "sample": f"{it} sweeps of the same graph (n={n}, m={m}) by gtc_oracle.c, "
+                         f"{threads} OpenMP threads, {dt:.2f} s"}
+        del g
+
+    if rank == 0:
+        out = {
+            "metric": "PageRank GTEPS", "value": value, "unit": "GTEPS", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {
+                "workload": args.workload, "graph": wl["label"], "n": n, "m": m,
+                "damping": DAMPING, "epsilon": wl["eps"], "sweeps_per_solve": iters_per_solve,
+                "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches), "sweep_launches": int(sweep_launches),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(out), flush=True)
+    _ffi.check(L.gtc_graph_destroy(h))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,344 @@
+// gtc_api.cu -- the C ABI (include/gtc.h): argument checks, error capture,
+// handle lifetime.  Every entry point catches everything; nothing unwinds
+// into the caller.
+#include <cmath>
+#include <cstring>
+#include <algorithm>
+#include <new>
+
+#include "gtc_view.cuh"
+
+namespace gtc {
+
+static thread_local std::string t_err;
+
+void set_error(const std::string& msg) { t_err = msg; }
+
+static void require_device() {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        (void)cudaGetLastError();
+        throw Error{GTC_ERR_NO_DEVICE,
+                    std::string("no usable CUDA device: ") +
+                        (e != cudaSuccess ? cudaGetErrorString(e) : "device count is 0")};
+    }
+}
+
+template <class F>
+static int guarded(F&& f) {
+    try {
+        f();
+        t_err.clear();
+        return GTC_OK;
+    } catch (const Error& e) {
+        t_err = e.msg;
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        t_err = "host allocation failed";
+        return GTC_ERR_OOM;
+    } catch (...) {
+        t_err = "unexpected internal error";
+        return GTC_ERR_CUDA;
+    }
+}
+
+static gtc_graph* new_graph(uint64_t n, uint64_t m) {
+    GTC_REQUIRE(n <= 0xFFFFFFFEull, GTC_ERR_ARG,
+                "vertex count exceeds the index space (MAX_INDEX = 2^32 - 2)");
+    GTC_REQUIRE(m <= 0xFFFFFFFEull, GTC_ERR_ARG,
+                "edge count exceeds the index space (MAX_INDEX = 2^32 - 2)");
+    require_device();
+    gtc_graph* g = new gtc_graph();
+    g->n = (uint32_t)n;
+    g->m = (uint32_t)m;
+    cudaError_t e = cudaGetDevice(&g->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->home, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete g;
+        throw Error{GTC_ERR_CUDA, std::string("stream creation failed: ") + cudaGetErrorString(e)};
+    }
+    g->stream = g->home;
+    return g;
+}
+
+static void destroy_graph(gtc_graph* g) {
+    if (!g) return;
+    cudaStream_t home = g->home;
+    if (g->stream != home) cudaStreamSynchronize(g->stream);
+    delete g;  // graph buffers are freed on the home stream
+    if (home) {
+        cudaStreamSynchronize(home);
+        cudaStreamDestroy(home);
+    }
+}
+
+static void check_params(const gtc_graph* g, const gtc_power_iteration* p, gtc_power_iteration& out) {
+    GTC_REQUIRE(p, GTC_ERR_ARG, "params is NULL");
+    out = *p;
+    GTC_REQUIRE(out.plan_len == g->n, GTC_ERR_ARG, "sweep: the plan must cover the output exactly");
+    if (out.plan_chunks == 0) out.plan_chunks = out.plan_len ? (out.plan_len + 4095) / 4096 : 1;
+    if (out.plan_chunks == 0) out.plan_chunks = 1;
+    GTC_REQUIRE(out.plan_chunks <= (out.plan_len ? out.plan_len : 1), GTC_ERR_ARG,
+                "plan has more chunks than items");
+    GTC_REQUIRE(!std::isnan(out.epsilon), GTC_ERR_ARG, "epsilon is NaN");
+}
+
+}  // namespace gtc
+
+using namespace gtc;
+
+extern "C" {
+
+const char* gtc_version(void) { return "gtc 0.1.0 (sm_103a)"; }
+
+const char* gtc_last_error(void) { return t_err.c_str(); }
+
+int gtc_graph_create_device(uint64_t n, uint64_t m, const uint32_t* d_src, const uint32_t* d_tgt,
+                            void* stream, gtc_graph** out) {
+    return guarded([&] {
+        GTC_REQUIRE(out, GTC_ERR_ARG, "out is NULL");
+        *out = nullptr;
+        GTC_REQUIRE(m == 0 || (d_src && d_tgt), GTC_ERR_ARG, "src/tgt is NULL");
+        gtc_graph* g = new_graph(n, m);
+        try {
+            cudaEvent_t ev = nullptr;
+            if (stream) {  // the caller's writes of src/tgt happen-before the build
+                GTC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+                GTC_CUDA(cudaEventRecord(ev, (cudaStream_t)stream));
+                GTC_CUDA(cudaStreamWaitEvent(g->home, ev, 0));
+                cudaEventDestroy(ev);
+            }
+            build_halves(g, d_src, d_tgt);
+        } catch (...) {
+            destroy_graph(g);
+            throw;
+        }
+        *out = g;
+    });
+}
+
+int gtc_graph_create(uint64_t n, uint64_t m, const uint32_t* src, const uint32_t* tgt,
+                     gtc_graph** out) {
+    return guarded([&] {
+        GTC_REQUIRE(out, GTC_ERR_ARG, "out is NULL");
+        *out = nullptr;
+        GTC_REQUIRE(m == 0 || (src && tgt), GTC_ERR_ARG, "src/tgt is NULL");
+        gtc_graph* g = new_graph(n, m);
+        try {
+            DevBuf<uint32_t> ds(m, g->home), dt(m, g->home);
+            if (m) {
+                GTC_CUDA(cudaMemcpyAsync(ds.get(), src, m * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                         g->home));
+                GTC_CUDA(cudaMemcpyAsync(dt.get(), tgt, m * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                         g->home));
+            }
+            build_halves(g, ds.get(), dt.get());
+        } catch (...) {
+            destroy_graph(g);
+            throw;
+        }
+        *out = g;
+    });
+}
+
+int gtc_graph_destroy(gtc_graph* g) {
+    return guarded([&] { destroy_graph(g); });
+}
+
+int gtc_graph_info(const gtc_graph* g, uint64_t* n, uint64_t* edge_bound, uint64_t* num_edges) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        if (n) *n = g->n;
+        if (edge_bound) *edge_bound = g->m;
+        if (num_edges) *num_edges = g->m;
+    });
+}
+
+int gtc_graph_export(const gtc_graph* g, uint64_t* out_off, uint32_t* out_other, uint32_t* out_idx,
+                     uint64_t* in_off, uint32_t* in_other, uint32_t* in_idx) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        cudaStream_t s = g->home;
+        const size_t n1 = (size_t)g->n + 1, m = g->m;
+        std::vector<uint32_t> tmp(n1);
+        auto offs = [&](const DevBuf<uint32_t>& d, uint64_t* h) {
+            if (!h) return;
+            GTC_CUDA(cudaMemcpyAsync(tmp.data(), d.get(), n1 * sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, s));
+            GTC_CUDA(cudaStreamSynchronize(s));
+            for (size_t i = 0; i < n1; ++i) h[i] = tmp[i];
+        };
+        auto arr = [&](const DevBuf<uint32_t>& d, uint32_t* h) {
+            if (h && m)
+                GTC_CUDA(cudaMemcpyAsync(h, d.get(), m * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        };
+        offs(g->out.off, out_off);
+        offs(g->in.off, in_off);
+        arr(g->out.other, out_other);
+        arr(g->out.eid, out_idx);
+        arr(g->in.other, in_other);
+        arr(g->in.eid, in_idx);
+        GTC_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int gtc_graph_set_stream(gtc_graph* g, void* stream) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        GTC_CUDA(cudaStreamSynchronize(g->stream));
+        GTC_CUDA(cudaStreamSynchronize(g->home));
+        g->stream = stream ? (cudaStream_t)stream : g->home;
+    });
+}
+
+static cudaStream_t stream_of(const gtc_graph* g, const gtc_options* opt) {
+    return (opt && opt->stream) ? (cudaStream_t)opt->stream : g->stream;
+}
+
+static void common_opts(const gtc_options* opt, SolveIn& in) {
+    in.precision = opt ? opt->precision : GTC_PREC_F32;
+    in.timing = opt && opt->timing;
+    GTC_REQUIRE(in.precision == GTC_PREC_F32 || in.precision == GTC_PREC_F64_EXACT, GTC_ERR_ARG,
+                "unknown precision");
+}
+
+static DVec dvec_in(const gtc_dvec* v, uint64_t need, const char* what) {
+    DVec d;
+    if (!v || !v->ptr) return d;
+    GTC_REQUIRE(v->dtype == GTC_F64 || v->dtype == GTC_F32, GTC_ERR_ARG,
+                std::string(what) + ": unknown dtype");
+    GTC_REQUIRE(v->len >= need, GTC_ERR_ARG,
+                std::string(what) + " map is shorter than its index bound");
+    d.p = v->ptr;
+    d.len = v->len;
+    d.dtype = v->dtype;
+    return d;
+}
+
+// Host arrays staged through device buffers around the device solve.
+struct HostStage {
+    DevBuf<double> w, p, x;
+};
+
+static void stage_host(gtc_graph* g, cudaStream_t s, const double* weight, const double* pers,
+                       double* x, uint64_t had, SolveIn& in, HostStage& st) {
+    const uint32_t n = g->n, m = g->m;
+    if (weight) {
+        st.w.alloc(m, s);
+        if (m) GTC_CUDA(cudaMemcpyAsync(st.w.get(), weight, (size_t)m * 8, cudaMemcpyHostToDevice, s));
+        in.weight = DVec{st.w.get(), m, GTC_F64};
+    }
+    if (pers) {
+        st.p.alloc(n, s);
+        if (n) GTC_CUDA(cudaMemcpyAsync(st.p.get(), pers, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+        in.pers = DVec{st.p.get(), n, GTC_F64};
+    }
+    st.x.alloc(n, s);
+    uint64_t k = std::min<uint64_t>(had, n);
+    if (k) GTC_CUDA(cudaMemcpyAsync(st.x.get(), x, (size_t)k * 8, cudaMemcpyHostToDevice, s));
+    in.x = st.x.get();
+    in.x_dtype = GTC_F64;
+    in.had = had;
+}
+
+static void unstage_host(gtc_graph* g, cudaStream_t s, double* x, HostStage& st) {
+    if (g->n)
+        GTC_CUDA(cudaMemcpyAsync(x, st.x.get(), (size_t)g->n * 8, cudaMemcpyDeviceToHost, s));
+    GTC_CUDA(cudaStreamSynchronize(s));
+}
+
+int gtc_pagerank(gtc_graph* g, const gtc_view* view, const double* weight, uint64_t weight_len,
+                 const double* pers, uint64_t pers_len, double damping,
+                 const gtc_power_iteration* params, double* rank, uint64_t rank_len,
+                 uint64_t rank_had, const gtc_options* opt, gtc_result* result) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        SolveIn in{};
+        check_params(g, params, in.params);
+        GTC_REQUIRE(!weight || weight_len >= g->m, GTC_ERR_ARG,
+                    "weight map is shorter than the edge bound");
+        GTC_REQUIRE(!pers || pers_len >= g->n, GTC_ERR_ARG,
+                    "personalisation map is shorter than the vertex bound");
+        GTC_REQUIRE(rank || g->n == 0, GTC_ERR_ARG, "rank is NULL");
+        GTC_REQUIRE(rank_len >= g->n, GTC_ERR_ARG, "rank map is shorter than the vertex bound");
+        GTC_REQUIRE(!std::isnan(damping), GTC_ERR_ARG, "damping is NaN");
+        common_opts(opt, in);
+        in.damping = damping;
+        cudaStream_t s = stream_of(g, opt);
+        HostStage st;
+        stage_host(g, s, weight, pers, rank, rank_had, in, st);
+        gtc_result r{};
+        gtc::pagerank(g, view, in, &r, s);
+        unstage_host(g, s, rank, st);
+        if (result) *result = r;
+    });
+}
+
+int gtc_eigenvector(gtc_graph* g, const gtc_view* view, const double* weight, uint64_t weight_len,
+                    const gtc_power_iteration* params, double* x, uint64_t x_len, uint64_t x_had,
+                    const gtc_options* opt, gtc_result* result) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        SolveIn in{};
+        check_params(g, params, in.params);
+        GTC_REQUIRE(!weight || weight_len >= g->m, GTC_ERR_ARG,
+                    "weight map is shorter than the edge bound");
+        GTC_REQUIRE(x || g->n == 0, GTC_ERR_ARG, "x is NULL");
+        GTC_REQUIRE(x_len >= g->n, GTC_ERR_ARG, "centrality map is shorter than the vertex bound");
+        common_opts(opt, in);
+        cudaStream_t s = stream_of(g, opt);
+        HostStage st;
+        stage_host(g, s, weight, nullptr, x, x_had, in, st);
+        gtc_result r{};
+        gtc::eigenvector(g, view, in, &r, s);
+        unstage_host(g, s, x, st);
+        if (result) *result = r;
+    });
+}
+
+int gtc_pagerank_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* weight,
+                        const gtc_dvec* pers, double damping, const gtc_power_iteration* params,
+                        gtc_dvec* rank, uint64_t rank_had, const gtc_options* opt,
+                        gtc_result* result) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        SolveIn in{};
+        check_params(g, params, in.params);
+        in.weight = dvec_in(weight, g->m, "weight");
+        in.pers = dvec_in(pers, g->n, "personalisation");
+        GTC_REQUIRE(rank && (rank->ptr || g->n == 0), GTC_ERR_ARG, "rank is NULL");
+        DVec x = dvec_in(rank, g->n, "rank");
+        GTC_REQUIRE(!std::isnan(damping), GTC_ERR_ARG, "damping is NaN");
+        common_opts(opt, in);
+        in.damping = damping;
+        in.x = rank->ptr;
+        in.x_dtype = x.p ? x.dtype : GTC_F64;
+        in.had = rank_had;
+        gtc_result r{};
+        gtc::pagerank(g, view, in, &r, stream_of(g, opt));
+        if (result) *result = r;
+    });
+}
+
+int gtc_eigenvector_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* weight,
+                           const gtc_power_iteration* params, gtc_dvec* x, uint64_t x_had,
+                           const gtc_options* opt, gtc_result* result) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        SolveIn in{};
+        check_params(g, params, in.params);
+        in.weight = dvec_in(weight, g->m, "weight");
+        GTC_REQUIRE(x && (x->ptr || g->n == 0), GTC_ERR_ARG, "x is NULL");
+        DVec xv = dvec_in(x, g->n, "centrality");
+        common_opts(opt, in);
+        in.x = x->ptr;
+        in.x_dtype = xv.p ? xv.dtype : GTC_F64;
+        in.had = x_had;
+        gtc_result r{};
+        gtc::eigenvector(g, view, in, &r, stream_of(g, opt));
+        if (result) *result = r;
+    });
+}
+
+}  // extern "C"

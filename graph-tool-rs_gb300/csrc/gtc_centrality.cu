@@ -1,0 +1,778 @@
+// gtc_centrality.cu -- PageRank and eigenvector centrality on one GB300.
+//
+// The sweeps of crates/gt-algo/src/centrality.rs, in two arithmetics:
+//
+// GTC_PREC_F32 (the fast path).  Vectors and edge weights in FP32, the row
+// sum of a pull as a compensated (TwoSum-based) FP32 sum, the dangling mass
+// and the L1 delta folded in FP64 across blocks.  PageRank pulls
+// y[s] = rank[s] / deg[s] (written by the previous sweep's epilogue), so the
+// edge loop is one index load, one gather and, when weighted, one weight
+// load per in-edge.  The sweep is fused: pull + damping + delta + next
+// sweep's dangling mass in one kernel, reduced deterministically (per-block
+// partials, folded in block order by the last block to finish).
+//
+// GTC_PREC_F64_EXACT.  The reference's arithmetic step for step: per-edge
+// `(prev[s] * w) / ds` (centrality.rs:361), `nv = (1-d)*pv + d*r` (:364), the
+// delta folded sequentially inside each Plan chunk and the chunk partials
+// left-folded from 0.0 (sweep, :141-167; det_reduce, reduce.rs:40-55).  IEEE
+// round-to-nearest intrinsics keep the compiler from fusing a multiply into
+// an add.  Results are bit-identical to the reference's for the same Plan.
+#include <algorithm>
+#include <cmath>
+
+#include "gtc_view.cuh"
+
+namespace gtc {
+
+// --------------------------------------------------------------------------
+// deterministic block reduction of two FP64 partials + last-block fold
+// --------------------------------------------------------------------------
+
+struct Fold2 {
+    double* part_a;    // [gridDim.x]
+    double* part_b;    // [gridDim.x]
+    unsigned* ticket;  // zero before the launch; the last block resets it
+    double* out_a;     // folded results
+    double* out_b;
+};
+
+// Block of NT threads; every thread passes its (a, b).  The last block to
+// finish folds all block partials in block order.
+template <int NT>
+__device__ __forceinline__ void block_fold2(double a, double b, const Fold2& f) {
+    __shared__ double sa[NT / 32], sb[NT / 32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    a = warp_sum_f64(a);
+    b = warp_sum_f64(b);
+    if (lane == 0) sa[warp] = a, sb[warp] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (int w = 0; w < NT / 32; ++w) ta += sa[w], tb += sb[w];
+        f.part_a[blockIdx.x] = ta;
+        f.part_b[blockIdx.x] = tb;
+        __threadfence();
+        unsigned t = atomicAdd(f.ticket, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && warp == 0) {
+        __threadfence();
+        double ta = 0.0, tb = 0.0;
+        for (unsigned i = lane; i < gridDim.x; i += 32) {
+            ta += __ldcg(f.part_a + i);
+            tb += __ldcg(f.part_b + i);
+        }
+        ta = warp_sum_f64(ta);
+        tb = warp_sum_f64(tb);
+        if (lane == 0) {
+            *f.out_a = ta;
+            *f.out_b = tb;
+            *f.ticket = 0u;
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// FP32 PageRank
+// --------------------------------------------------------------------------
+
+struct PrF32 {
+    uint32_t n;
+    const uint32_t* __restrict__ off;    // pull offsets (n+1)
+    const uint32_t* __restrict__ other;  // pull sources
+    const float* __restrict__ w;         // pull-ordered weights or null
+    const float* __restrict__ invdeg;    // 1/deg, 0 for sinks and inactive
+    const uint8_t* __restrict__ sink;    // active && deg == 0
+    const uint8_t* __restrict__ active;  // null = all
+    const float* __restrict__ pers;      // null = uniform
+    float uniform;
+    float one_minus_d, d;
+    const double* psink;  // dangling mass of prev
+    const float* __restrict__ prev;
+    const float* __restrict__ yprev;
+    float* __restrict__ next;
+    float* __restrict__ ynext;
+    Fold2 fold;  // a = delta, b = dangling mass of next
+};
+
+constexpr int PR_NT = 256;
+
+// One warp per row (grid-stride).  Lanes stride the row's in-edges with a
+// compensated sum, merged across the warp with TwoSum.
+template <bool WEIGHTED>
+__global__ void __launch_bounds__(PR_NT) k_pr_f32_warp(PrF32 a) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * PR_NT + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * PR_NT) >> 5;
+    const float psink = (float)*a.psink;
+    Kahan dacc, sacc;
+    for (uint32_t row = gw; row < a.n; row += nw) {
+        if (a.active && !a.active[row]) {
+            if (lane == 0) {
+                a.next[row] = a.prev[row];
+                a.ynext[row] = 0.f;
+            }
+            continue;
+        }
+        const uint32_t b = a.off[row], e = a.off[row + 1];
+        Kahan k;
+        for (uint32_t p = b + lane; p < e; p += 32) {
+            float x = a.yprev[a.other[p]];
+            if (WEIGHTED) x = __fmul_rn(x, a.w[p]);
+            k.add(x);
+        }
+        warp_merge_kahan(k);
+        if (lane == 0) {
+            const float pv = a.pers ? a.pers[row] : a.uniform;
+            const float r = __fadd_rn(__fmul_rn(psink, pv), k.value());
+            const float nv = __fadd_rn(__fmul_rn(a.one_minus_d, pv), __fmul_rn(a.d, r));
+            const float pr = a.prev[row];
+            a.next[row] = nv;
+            a.ynext[row] = __fmul_rn(nv, a.invdeg[row]);
+            dacc.add(fabsf(__fsub_rn(nv, pr)));
+            if (a.sink[row]) sacc.add(nv);
+        }
+    }
+    block_fold2<PR_NT>((double)dacc.s + (double)dacc.c, (double)sacc.s + (double)sacc.c, a.fold);
+}
+
+// --------------------------------------------------------------------------
+// per-call preparation kernels
+// --------------------------------------------------------------------------
+
+// deg[v]: Unity -> the view's out-degree; weighted -> a left fold of the
+// view's out-edge weights in storage order, FP64, as centrality.rs:281-297.
+__global__ void k_degree(uint32_t n, const uint32_t* __restrict__ push_off,
+                         const uint32_t* __restrict__ push_eid, const void* __restrict__ w,
+                         int wdt, const uint8_t* __restrict__ active, double* __restrict__ deg,
+                         uint8_t* __restrict__ sink) {
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const uint32_t b = push_off[v], e = push_off[v + 1];
+    double k;
+    if (!w) {
+        k = (double)(e - b);
+    } else {
+        k = 0.0;
+        for (uint32_t p = b; p < e; ++p) k = __dadd_rn(k, ld_any(w, wdt, push_eid[p]));
+    }
+    const bool act = !active || active[v];
+    deg[v] = act ? k : 0.0;
+    sink[v] = (act && k == 0.0) ? 1 : 0;
+}
+
+__global__ void k_invdeg_f32(uint32_t n, const double* __restrict__ deg,
+                             float* __restrict__ invdeg) {
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) invdeg[v] = deg[v] != 0.0 ? (float)(1.0 / deg[v]) : 0.f;
+}
+
+// Weights into pull order (the order the sweep streams them).
+template <class T>
+__global__ void k_gather_w(uint32_t m, const uint32_t* __restrict__ eid,
+                           const void* __restrict__ w, int wdt, T* __restrict__ out) {
+    size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < m) out[p] = (T)ld_any(w, wdt, eid[p]);
+}
+
+// Initial iterate (FP64): slots below `had` come from the caller's map, the
+// rest are seeded (seed_new_slots, centrality.rs:198-205).
+__global__ void k_seed(uint32_t n, uint64_t had, const void* __restrict__ x, int xdt,
+                       const void* __restrict__ pers, int pdt, double uniform,
+                       double* __restrict__ x64) {
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    x64[v] = v < had ? ld_any(x, xdt, v) : (pers ? ld_any(pers, pdt, v) : uniform);
+}
+
+__global__ void k_to_f32(uint32_t n, const void* __restrict__ x, int xdt, float* __restrict__ y) {
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) y[v] = (float)ld_any(x, xdt, v);
+}
+
+// Store an iterate into the caller's map, in the map's type.
+template <class T>
+__global__ void k_store(uint32_t n, const T* __restrict__ src, void* __restrict__ x, int xdt) {
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    if (xdt == GTC_F64)
+        ((double*)x)[v] = (double)src[v];
+    else
+        ((float*)x)[v] = (float)src[v];
+}
+
+// y = rank * invdeg, plus the dangling mass of rank (block-folded).
+__global__ void __launch_bounds__(PR_NT) k_pr_prime(uint32_t n, const float* __restrict__ r,
+                                                   const float* __restrict__ invdeg,
+                                                   const uint8_t* __restrict__ sink,
+                                                   float* __restrict__ y, Fold2 f) {
+    Kahan sacc;
+    for (size_t v = (size_t)blockIdx.x * PR_NT + threadIdx.x; v < n;
+         v += (size_t)gridDim.x * PR_NT) {
+        float x = r[v];
+        y[v] = __fmul_rn(x, invdeg[v]);
+        if (sink[v]) sacc.add(x);
+    }
+    block_fold2<PR_NT>(0.0, (double)sacc.s + (double)sacc.c, f);
+}
+
+// --------------------------------------------------------------------------
+// FP64 exact kernels
+// --------------------------------------------------------------------------
+
+// Plan::range (plan.rs:88-101)
+__device__ __forceinline__ void plan_range(uint64_t n, uint64_t chunks, uint64_t k, uint64_t& s,
+                                           uint64_t& e) {
+    uint64_t base = n / chunks, rem = n % chunks;
+    s = k * base + (k < rem ? k : rem);
+    e = s + base + (k < rem ? 1 : 0);
+}
+
+// One thread per row, the in-edge loop sequential in storage order.
+__global__ void k_pr_f64_rows(uint32_t n, const uint32_t* __restrict__ off,
+                              const uint32_t* __restrict__ other, const double* __restrict__ w,
+                              const double* __restrict__ deg, const uint8_t* __restrict__ active,
+                              const double* __restrict__ pers, double uniform, double one_minus_d,
+                              double d, const double* __restrict__ psink_p,
+                              const double* __restrict__ prev, double* __restrict__ next,
+                              double* __restrict__ diff) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (active && !active[i]) {
+        next[i] = prev[i];
+        diff[i] = 0.0;
+        return;
+    }
+    const double p_sink = *psink_p;
+    const double pv = pers ? pers[i] : uniform;
+    double r = __dmul_rn(p_sink, pv);
+    for (uint32_t p = off[i], e = off[i + 1]; p < e; ++p) {
+        const uint32_t s = other[p];
+        const double ds = deg[s];
+        if (ds != 0.0) {
+            const double we = w ? w[p] : 1.0;
+            r = __dadd_rn(r, __ddiv_rn(__dmul_rn(prev[s], we), ds));
+        }
+    }
+    const double nv = __dadd_rn(__dmul_rn(one_minus_d, pv), __dmul_rn(d, r));
+    diff[i] = fabs(__dsub_rn(nv, prev[i]));
+    next[i] = nv;
+}
+
+// Plan-chunk partials: thread k folds its chunk sequentially from 0.0.
+__global__ void k_chunk_sums(uint64_t n, uint64_t chunks, const double* __restrict__ v,
+                             const uint32_t* __restrict__ gather, double* __restrict__ part) {
+    uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= chunks) return;
+    uint64_t s, e;
+    plan_range(n, chunks, k, s, e);
+    double acc = 0.0;
+    for (uint64_t i = s; i < e; ++i) acc = __dadd_rn(acc, gather ? v[gather[i]] : v[i]);
+    part[k] = acc;
+}
+
+// Left fold of the chunk partials from 0.0 (one thread).  mode 0: out = sum;
+// mode 1: out = sum and out2 = the eigenvector scale (sqrt, 1 if zero).
+__global__ void k_fold(uint64_t chunks, const double* __restrict__ part, double* out,
+                       double* out2, int mode) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double acc = 0.0;
+    for (uint64_t k = 0; k < chunks; ++k) acc = __dadd_rn(acc, part[k]);
+    *out = acc;
+    if (mode == 1) {
+        double norm = __dsqrt_rn(acc);
+        out[1] = norm;
+        *out2 = norm == 0.0 ? 1.0 : norm;
+    }
+}
+
+__global__ void k_compact_sinks(uint32_t n, const uint8_t* __restrict__ sink,
+                                const uint32_t* __restrict__ pos, uint32_t* __restrict__ list) {
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n && sink[v]) list[pos[v]] = (uint32_t)v;
+}
+
+__global__ void k_u8_to_u32(uint32_t n, const uint8_t* __restrict__ a, uint32_t* __restrict__ b) {
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) b[v] = a[v];
+}
+
+// Eigenvector sweep 1 (centrality.rs:446-465): s = sum w*prev[other] in
+// storage order, sq[i] = s*s.
+__global__ void k_ev_f64_rows(uint32_t n, const uint32_t* __restrict__ off,
+                              const uint32_t* __restrict__ other, const double* __restrict__ w,
+                              const uint8_t* __restrict__ active, const double* __restrict__ prev,
+                              double* __restrict__ next, double* __restrict__ sq) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (active && !active[i]) {
+        next[i] = prev[i];
+        sq[i] = 0.0;
+        return;
+    }
+    double s = 0.0;
+    for (uint32_t p = off[i], e = off[i + 1]; p < e; ++p) {
+        const double we = w ? w[p] : 1.0;
+        s = __dadd_rn(s, __dmul_rn(we, prev[other[p]]));
+    }
+    next[i] = s;
+    sq[i] = __dmul_rn(s, s);
+}
+
+// Eigenvector sweep 2 (centrality.rs:472-484): next /= scale, |next - prev|.
+__global__ void k_ev_f64_norm(uint32_t n, const uint8_t* __restrict__ active,
+                              const double* __restrict__ scale_p, const double* __restrict__ prev,
+                              double* __restrict__ next, double* __restrict__ diff) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (active && !active[i]) {
+        diff[i] = 0.0;
+        return;
+    }
+    const double x = __ddiv_rn(next[i], *scale_p);
+    next[i] = x;
+    diff[i] = fabs(__dsub_rn(x, prev[i]));
+}
+
+// --------------------------------------------------------------------------
+// FP32 eigenvector
+// --------------------------------------------------------------------------
+
+struct EvF32 {
+    uint32_t n;
+    const uint32_t* __restrict__ off;
+    const uint32_t* __restrict__ other;
+    const float* __restrict__ w;
+    const uint8_t* __restrict__ active;
+    const float* __restrict__ prev;
+    float* __restrict__ next;
+    Fold2 fold;  // a = squared norm
+};
+
+template <bool WEIGHTED>
+__global__ void __launch_bounds__(PR_NT) k_ev_f32_warp(EvF32 a) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * PR_NT + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * PR_NT) >> 5;
+    Kahan qacc;
+    for (uint32_t row = gw; row < a.n; row += nw) {
+        if (a.active && !a.active[row]) {
+            if (lane == 0) a.next[row] = a.prev[row];
+            continue;
+        }
+        const uint32_t b = a.off[row], e = a.off[row + 1];
+        Kahan k;
+        for (uint32_t p = b + lane; p < e; p += 32) {
+            float x = a.prev[a.other[p]];
+            if (WEIGHTED) x = __fmul_rn(a.w[p], x);
+            k.add(x);
+        }
+        warp_merge_kahan(k);
+        if (lane == 0) {
+            const float s = k.value();
+            a.next[row] = s;
+            qacc.add(__fmul_rn(s, s));
+        }
+    }
+    block_fold2<PR_NT>((double)qacc.s + (double)qacc.c, 0.0, a.fold);
+}
+
+// next /= scale (scale from the FP64 norm, 1 if zero) and the FP64 delta.
+__global__ void __launch_bounds__(PR_NT) k_ev_f32_norm(uint32_t n,
+                                                      const uint8_t* __restrict__ active,
+                                                      const double* __restrict__ sqnorm,
+                                                      const float* __restrict__ prev,
+                                                      float* __restrict__ next, Fold2 f) {
+    const double norm = sqrt(*sqnorm);
+    const float inv = (float)(1.0 / (norm == 0.0 ? 1.0 : norm));
+    Kahan dacc;
+    for (size_t v = (size_t)blockIdx.x * PR_NT + threadIdx.x; v < n;
+         v += (size_t)gridDim.x * PR_NT) {
+        if (active && !active[v]) continue;
+        const float x = __fmul_rn(next[v], inv);
+        next[v] = x;
+        dacc.add(fabsf(__fsub_rn(x, prev[v])));
+    }
+    block_fold2<PR_NT>((double)dacc.s + (double)dacc.c, 0.0, f);
+}
+
+// --------------------------------------------------------------------------
+// host drivers
+// --------------------------------------------------------------------------
+
+namespace {
+
+struct Timer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaStream_t s;
+    explicit Timer(cudaStream_t st) : s(st) {
+        GTC_CUDA(cudaEventCreate(&a));
+        GTC_CUDA(cudaEventCreate(&b));
+    }
+    ~Timer() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+    void start() { GTC_CUDA(cudaEventRecord(a, s)); }
+    void stop() { GTC_CUDA(cudaEventRecord(b, s)); }
+    // after the stream has passed stop()
+    double ms() {
+        GTC_CUDA(cudaEventSynchronize(b));
+        float t = 0.f;
+        GTC_CUDA(cudaEventElapsedTime(&t, a, b));
+        return t;
+    }
+};
+
+// Reduction scratch for one launch shape.
+struct FoldBufs {
+    DevBuf<double> pa, pb, out;
+    DevBuf<unsigned> ticket;
+    FoldBufs(unsigned blocks, cudaStream_t s)
+        : pa(blocks, s), pb(blocks, s), out(4, s), ticket(1, s) {
+        GTC_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), s));
+        GTC_CUDA(cudaMemsetAsync(out.get(), 0, 4 * sizeof(double), s));
+    }
+    Fold2 fold(double* oa, double* ob) { return Fold2{pa.get(), pb.get(), ticket.get(), oa, ob}; }
+};
+
+unsigned persistent_blocks(uint32_t rows) {
+    // one row per warp, at most 152 SMs x 8 resident blocks of 256 threads
+    unsigned want = (rows + (PR_NT / 32) - 1) / (PR_NT / 32);
+    unsigned cap = kSMs * 8;
+    return want < 1 ? 1 : (want > cap ? cap : want);
+}
+
+// Everything a sweep loop needs that does not change between sweeps.
+struct Prep {
+    View view;
+    double uniform = 0.0;
+    DevBuf<double> deg;
+    DevBuf<uint8_t> sink;
+    DevBuf<double> x64;  // initial iterate, FP64
+};
+
+void prepare(gtc_graph* g, const gtc_view* vw, const SolveIn& in, bool need_deg, Prep& P,
+             cudaStream_t s, uint64_t* L) {
+    const unsigned TB = 256;
+    P.view.prepare(g, vw, s, L);
+    const uint32_t n = P.view.n;
+    P.uniform = P.view.n_active == 0 ? 0.0 : 1.0 / (double)P.view.n_active;
+    if (need_deg) {
+        P.deg.alloc(n, s);
+        P.sink.alloc(n, s);
+        if (n) {
+            k_degree<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(
+                n, P.view.push_off, P.view.push_eid, in.weight.p, in.weight.dtype,
+                P.view.active_or_null(), P.deg.get(), P.sink.get());
+            GTC_LAUNCHED();
+            (*L)++;
+        }
+    }
+    P.x64.alloc(n, s);
+    if (n) {
+        k_seed<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, in.had, in.x, in.x_dtype, in.pers.p,
+                                                        in.pers.dtype, P.uniform, P.x64.get());
+        GTC_LAUNCHED();
+        (*L)++;
+    }
+}
+
+template <class T>
+void store_result(uint32_t n, const T* src, const SolveIn& in, cudaStream_t s, uint64_t* L) {
+    if (!n) return;
+    k_store<T><<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, src, in.x, in.x_dtype);
+    GTC_LAUNCHED();
+    (*L)++;
+}
+
+template <class T>
+DevBuf<T> pull_weights(const Prep& P, const SolveIn& in, cudaStream_t s, uint64_t* L) {
+    DevBuf<T> w;
+    const uint32_t mp = P.view.m_pull;
+    if (in.weight.present() && mp) {
+        w.alloc(mp, s);
+        k_gather_w<T><<<grid_for(mp, 256, 1u << 30), 256, 0, s>>>(mp, P.view.pull_eid, in.weight.p,
+                                                                 in.weight.dtype, w.get());
+        GTC_LAUNCHED();
+        (*L)++;
+    }
+    return w;
+}
+
+}  // namespace
+
+void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* res,
+              cudaStream_t s) {
+    uint64_t L = 0, SL = 0;
+    const unsigned TB = 256;
+    Prep P;
+    prepare(g, vw, in, true, P, s, &L);
+    const View& view = P.view;
+    const uint32_t n = view.n;
+    const double d = in.damping;
+    const uint8_t* act = view.active_or_null();
+    const uint64_t max_iter = in.params.max_iter;
+    const double eps = in.params.epsilon;
+    uint64_t iter = 0;
+    double delta = eps + 1.0, sweep_ms = 0.0;
+    Timer total(s), sw(s);
+
+    if (in.precision == GTC_PREC_F64_EXACT) {
+        const uint64_t chunks = in.params.plan_chunks;
+        // sinks in vertex order and their Plan (grain_of, centrality.rs:186-188, :311)
+        DevBuf<uint32_t> flag32(n, s), pos((size_t)n + 1, s);
+        if (n) {
+            k_u8_to_u32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.sink.get(), flag32.get());
+            GTC_LAUNCHED();
+            L++;
+        }
+        scan_exclusive_u32(flag32.get(), pos.get(), n, s, &L);
+        uint32_t n_sinks = 0;
+        GTC_CUDA(cudaMemcpyAsync(&n_sinks, pos.get() + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+        DevBuf<uint32_t> sinks(n_sinks, s);
+        if (n) {
+            k_compact_sinks<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.sink.get(), pos.get(),
+                                                                     sinks.get());
+            GTC_LAUNCHED();
+            L++;
+        }
+        const uint64_t grain = std::max<uint64_t>((n + chunks - 1) / chunks, 1);
+        const uint64_t sink_chunks = std::max<uint64_t>((n_sinks + grain - 1) / grain, 1);
+        DevBuf<double> wpull = pull_weights<double>(P, in, s, &L);
+        DevBuf<double> scratch(n, s), diff(n, s), part(std::max(chunks, sink_chunks), s);
+        DevBuf<double> scal(4, s);  // [p_sink, delta]
+        const double* pers64 = nullptr;
+        DevBuf<double> pbuf;
+        if (in.pers.present()) {
+            if (in.pers.dtype == GTC_F64) {
+                pers64 = (const double*)in.pers.p;
+            } else {
+                pbuf.alloc(n, s);
+                k_seed<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, n, in.pers.p, in.pers.dtype,
+                                                                nullptr, 0, 0.0, pbuf.get());
+                GTC_LAUNCHED();
+                L++;
+                pers64 = pbuf.get();
+            }
+        }
+        double* cur = P.x64.get();
+        double* nxt = scratch.get();
+        total.start();
+        while (delta >= eps) {
+            if (in.timing) sw.start();
+            k_chunk_sums<<<grid_for(sink_chunks, 128, 1u << 30), 128, 0, s>>>(
+                n_sinks, sink_chunks, cur, sinks.get(), part.get());
+            k_fold<<<1, 32, 0, s>>>(sink_chunks, part.get(), scal.get(), nullptr, 0);
+            if (n)
+                k_pr_f64_rows<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(
+                    n, view.pull_off, view.pull_other, wpull.get(), P.deg.get(), act, pers64,
+                    P.uniform, 1.0 - d, d, scal.get(), cur, nxt, diff.get());
+            k_chunk_sums<<<grid_for(chunks, 128, 1u << 30), 128, 0, s>>>(n, chunks, diff.get(),
+                                                                         nullptr, part.get());
+            k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get() + 1, nullptr, 0);
+            GTC_LAUNCHED();
+            if (in.timing) sw.stop();
+            L += n ? 5 : 4;
+            SL += n ? 5 : 4;
+            GTC_CUDA(cudaMemcpyAsync(&delta, scal.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+            GTC_CUDA(cudaStreamSynchronize(s));
+            if (in.timing) sweep_ms += sw.ms();
+            std::swap(cur, nxt);
+            iter++;
+            if (max_iter > 0 && iter == max_iter) break;
+        }
+        total.stop();
+        res->device_ms = total.ms();
+        store_result<double>(n, cur, in, s, &L);
+    } else {
+        DevBuf<float> invdeg(n, s);
+        if (n) {
+            k_invdeg_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.deg.get(), invdeg.get());
+            GTC_LAUNCHED();
+            L++;
+        }
+        DevBuf<float> wpull = pull_weights<float>(P, in, s, &L);
+        DevBuf<float> pers32;
+        if (in.pers.present() && n) {
+            pers32.alloc(n, s);
+            k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, in.pers.p, in.pers.dtype,
+                                                              pers32.get());
+            GTC_LAUNCHED();
+            L++;
+        }
+        DevBuf<float> r0(n, s), r1(n, s), y0(n, s), y1(n, s);
+        if (n) {
+            k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.x64.get(), GTC_F64, r0.get());
+            GTC_LAUNCHED();
+            L++;
+        }
+        const unsigned nb = persistent_blocks(n);
+        FoldBufs fb(nb, s);
+        double* dp = fb.out.get();  // [0] delta, [1] dangling mass of the current iterate
+        k_pr_prime<<<nb, PR_NT, 0, s>>>(n, r0.get(), invdeg.get(), P.sink.get(), y0.get(),
+                                       fb.fold(dp + 2, dp + 1));
+        GTC_LAUNCHED();
+        L++;
+        float *rc = r0.get(), *rn = r1.get(), *yc = y0.get(), *yn = y1.get();
+        PrF32 a;
+        a.n = n;
+        a.off = view.pull_off;
+        a.other = view.pull_other;
+        a.w = wpull.get();
+        a.invdeg = invdeg.get();
+        a.sink = P.sink.get();
+        a.active = act;
+        a.pers = pers32.get();
+        a.uniform = (float)P.uniform;
+        a.one_minus_d = (float)(1.0 - d);
+        a.d = (float)d;
+        a.psink = dp + 1;
+        a.fold = fb.fold(dp + 0, dp + 1);
+        total.start();
+        while (delta >= eps) {
+            a.prev = rc, a.yprev = yc, a.next = rn, a.ynext = yn;
+            if (in.timing) sw.start();
+            if (in.weight.present())
+                k_pr_f32_warp<true><<<nb, PR_NT, 0, s>>>(a);
+            else
+                k_pr_f32_warp<false><<<nb, PR_NT, 0, s>>>(a);
+            GTC_LAUNCHED();
+            if (in.timing) sw.stop();
+            L++;
+            SL++;
+            GTC_CUDA(cudaMemcpyAsync(&delta, dp, sizeof(double), cudaMemcpyDeviceToHost, s));
+            GTC_CUDA(cudaStreamSynchronize(s));
+            if (in.timing) sweep_ms += sw.ms();
+            std::swap(rc, rn);
+            std::swap(yc, yn);
+            iter++;
+            if (max_iter > 0 && iter == max_iter) break;
+        }
+        total.stop();
+        res->device_ms = total.ms();
+        store_result<float>(n, rc, in, s, &L);
+    }
+    GTC_CUDA(cudaStreamSynchronize(s));
+    res->iterations = iter;
+    res->last_delta = iter ? delta : 0.0;
+    res->eigenvalue = 0.0;
+    res->launches = L;
+    res->sweep_ms = sweep_ms;
+    res->sweep_launches = SL;
+    g->launches += L;
+}
+
+void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* res,
+                 cudaStream_t s) {
+    uint64_t L = 0, SL = 0;
+    Prep P;
+    prepare(g, vw, in, false, P, s, &L);
+    const View& view = P.view;
+    const uint32_t n = view.n;
+    const uint8_t* act = view.active_or_null();
+    const uint64_t max_iter = in.params.max_iter;
+    const double eps = in.params.epsilon;
+    uint64_t iter = 0;
+    double delta = eps + 1.0, norm = 0.0, sweep_ms = 0.0;
+    Timer total(s), sw(s);
+    if (in.precision == GTC_PREC_F64_EXACT) {
+        const uint64_t chunks = in.params.plan_chunks;
+        DevBuf<double> wpull = pull_weights<double>(P, in, s, &L);
+        DevBuf<double> scratch(n, s), tmp(n, s), part(chunks, s), scal(4, s);
+        double* cur = P.x64.get();
+        double* nxt = scratch.get();
+        total.start();
+        while (delta >= eps) {
+            if (in.timing) sw.start();
+            if (n)
+                k_ev_f64_rows<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(
+                    n, view.pull_off, view.pull_other, wpull.get(), act, cur, nxt, tmp.get());
+            k_chunk_sums<<<grid_for(chunks, 128, 1u << 30), 128, 0, s>>>(n, chunks, tmp.get(),
+                                                                         nullptr, part.get());
+            // scal[0] = squared norm, scal[1] = norm, scal[2] = scale
+            k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get(), scal.get() + 2, 1);
+            if (n)
+                k_ev_f64_norm<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(n, act, scal.get() + 2,
+                                                                         cur, nxt, tmp.get());
+            k_chunk_sums<<<grid_for(chunks, 128, 1u << 30), 128, 0, s>>>(n, chunks, tmp.get(),
+                                                                         nullptr, part.get());
+            k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get() + 3, nullptr, 0);
+            GTC_LAUNCHED();
+            if (in.timing) sw.stop();
+            L += n ? 6 : 4;
+            SL += n ? 6 : 4;
+            double hs[4];
+            GTC_CUDA(cudaMemcpyAsync(hs, scal.get(), 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+            GTC_CUDA(cudaStreamSynchronize(s));
+            if (in.timing) sweep_ms += sw.ms();
+            norm = hs[1];
+            delta = hs[3];
+            std::swap(cur, nxt);
+            iter++;
+            if (max_iter > 0 && iter == max_iter) break;
+        }
+        total.stop();
+        res->device_ms = total.ms();
+        store_result<double>(n, cur, in, s, &L);
+    } else {
+        DevBuf<float> wpull = pull_weights<float>(P, in, s, &L);
+        DevBuf<float> x0(n, s), x1(n, s);
+        if (n) {
+            k_to_f32<<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, P.x64.get(), GTC_F64, x0.get());
+            GTC_LAUNCHED();
+            L++;
+        }
+        const unsigned nb = persistent_blocks(n);
+        FoldBufs f1(nb, s), f2(nb, s);
+        double* o1 = f1.out.get();
+        double* o2 = f2.out.get();
+        float *xc = x0.get(), *xn = x1.get();
+        EvF32 a;
+        a.n = n;
+        a.off = view.pull_off;
+        a.other = view.pull_other;
+        a.w = wpull.get();
+        a.active = act;
+        a.fold = f1.fold(o1, o1 + 1);
+        total.start();
+        while (delta >= eps) {
+            a.prev = xc, a.next = xn;
+            if (in.timing) sw.start();
+            if (in.weight.present())
+                k_ev_f32_warp<true><<<nb, PR_NT, 0, s>>>(a);
+            else
+                k_ev_f32_warp<false><<<nb, PR_NT, 0, s>>>(a);
+            k_ev_f32_norm<<<nb, PR_NT, 0, s>>>(n, act, o1, xc, xn, f2.fold(o2, o2 + 1));
+            GTC_LAUNCHED();
+            if (in.timing) sw.stop();
+            L += 2;
+            SL += 2;
+            double sq = 0.0;
+            GTC_CUDA(cudaMemcpyAsync(&sq, o1, sizeof(double), cudaMemcpyDeviceToHost, s));
+            GTC_CUDA(cudaMemcpyAsync(&delta, o2, sizeof(double), cudaMemcpyDeviceToHost, s));
+            GTC_CUDA(cudaStreamSynchronize(s));
+            if (in.timing) sweep_ms += sw.ms();
+            norm = std::sqrt(sq);
+            std::swap(xc, xn);
+            iter++;
+            if (max_iter > 0 && iter == max_iter) break;
+        }
+        total.stop();
+        res->device_ms = total.ms();
+        store_result<float>(n, xc, in, s, &L);
+    }
+    GTC_CUDA(cudaStreamSynchronize(s));
+    res->iterations = iter;
+    res->last_delta = iter ? delta : 0.0;
+    res->eigenvalue = norm;
+    res->launches = L;
+    res->sweep_ms = sweep_ms;
+    res->sweep_launches = SL;
+    g->launches += L;
+}
+
+}  // namespace gtc

@@ -1,0 +1,224 @@
+// gtc_internal.cuh -- shared internals of libgtc (CUDA, sm_103a).
+//
+// Everything here is private to the library: the public surface is the C ABI
+// in include/gtc.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "gtc.h"
+
+namespace gtc {
+
+// --------------------------------------------------------------------------
+// errors
+// --------------------------------------------------------------------------
+
+// Per-thread message of the last failing call (gtc_last_error()).
+void set_error(const std::string& msg);
+
+struct Error {
+    int status;
+    std::string msg;
+};
+
+#define GTC_CUDA(call)                                                              \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess)                                                      \
+            throw ::gtc::Error{GTC_ERR_CUDA, std::string(#call) + ": " +            \
+                                                 cudaGetErrorString(e_)};           \
+    } while (0)
+
+#define GTC_REQUIRE(cond, status, msg)                                              \
+    do {                                                                            \
+        if (!(cond)) throw ::gtc::Error{(status), (msg)};                           \
+    } while (0)
+
+// Launch check: a launch error is reported, a pending asynchronous fault is
+// left for the next synchronising call to report.
+#define GTC_LAUNCHED() GTC_CUDA(cudaGetLastError())
+
+// --------------------------------------------------------------------------
+// device buffers
+// --------------------------------------------------------------------------
+
+// A stream-ordered device allocation released when the owner goes out of
+// scope.  Graph-lifetime arrays and per-call scratch both use it.
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaStream_t s = nullptr;
+    DevBuf() = default;
+    DevBuf(size_t count, cudaStream_t stream) { alloc(count, stream); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr, o.n = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p, n = o.n, s = o.s;
+            o.p = nullptr, o.n = 0;
+        }
+        return *this;
+    }
+    void alloc(size_t count, cudaStream_t stream) {
+        release();
+        s = stream;
+        n = count;
+        size_t bytes = (count ? count : 1) * sizeof(T);
+        cudaError_t e = cudaMallocAsync((void**)&p, bytes, s);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            (void)cudaGetLastError();
+            throw Error{e == cudaErrorMemoryAllocation ? GTC_ERR_OOM : GTC_ERR_CUDA,
+                        std::string("device allocation of ") + std::to_string(bytes) +
+                            " bytes failed: " + cudaGetErrorString(e)};
+        }
+    }
+    void release() {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+        n = 0;
+    }
+    ~DevBuf() { release(); }
+    T* get() const { return p; }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// --------------------------------------------------------------------------
+// graph
+// --------------------------------------------------------------------------
+
+// One direction of the adjacency, flattened: the block halves of every vertex
+// in storage order.  off has n+1 entries; other/eid have m.
+struct Halves {
+    DevBuf<uint32_t> off, other, eid;
+};
+
+// Pull schedule of one direction: the rows cut into work units of about
+// equal (rows + entries), computed once per graph.
+struct Schedule {
+    DevBuf<uint2> units;  // see gtc_pagerank.cu: {row_begin, row_end|LONG_FLAG} or chunk
+    uint32_t n_units = 0;
+    uint32_t cap = 0;     // merge items per unit the schedule was cut for
+};
+
+}  // namespace gtc
+
+struct gtc_graph {
+    int device = 0;
+    uint32_t n = 0;  // vertex bound
+    uint32_t m = 0;  // edge bound == live edges (ids 0..m-1)
+    cudaStream_t home = nullptr;    // owned; graph-lifetime buffers live on it
+    cudaStream_t stream = nullptr;  // where solves run (home, or the caller's)
+    gtc::Halves out;  // CSR: out-halves (out_edges order)
+    gtc::Halves in;   // CSC: in-halves (in_edges order, the pull order)
+    gtc::Schedule sched_in, sched_out;
+    uint64_t launches = 0;  // kernels this handle has launched (diagnostics)
+};
+
+namespace gtc {
+
+// graph build (gtc_build.cu)
+void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt);
+void build_schedule(gtc_graph* g, bool in_dir, uint32_t cap);
+
+// A device vector of either float type.
+struct DVec {
+    const void* p = nullptr;
+    uint64_t len = 0;
+    int dtype = GTC_F64;
+    bool present() const { return p != nullptr; }
+};
+
+// One solve's inputs, after the C ABI checked them.  Every vector is in
+// device memory.
+struct SolveIn {
+    DVec weight;                 // by EdgeId, or absent (Unity)
+    DVec pers;                   // by vertex index, or absent (uniform)
+    double damping = 0.85;
+    gtc_power_iteration params;  // plan_chunks resolved (never 0)
+    void* x = nullptr;           // initial iterate and output
+    int x_dtype = GTC_F64;
+    uint64_t had = 0;            // slots the caller's map already had
+    int precision = GTC_PREC_F32;
+    bool timing = false;
+};
+
+__device__ __forceinline__ double ld_any(const void* p, int dtype, size_t i) {
+    return dtype == GTC_F64 ? ((const double*)p)[i] : (double)((const float*)p)[i];
+}
+
+// solves (gtc_centrality.cu)
+void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* res,
+              cudaStream_t s);
+void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* res,
+                 cudaStream_t s);
+
+// scans (gtc_build.cu): exclusive scan of n u32 values into out[0..n],
+// out[n] = total.  `out` may alias `in` only if the caller passes the same
+// pointer for both.
+void scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s,
+                        uint64_t* launches);
+
+// --------------------------------------------------------------------------
+// device helpers
+// --------------------------------------------------------------------------
+
+// Knuth's TwoSum: s + e == a + b exactly (round-to-nearest).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Compensated (Kahan-Babuska / Neumaier) accumulator in f32.
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        float t, e;
+        two_sum(s, x, t, e);
+        s = t;
+        c = __fadd_rn(c, e);
+    }
+    // merge another compensated partial
+    __device__ __forceinline__ void merge(float os, float oc) {
+        float t, e;
+        two_sum(s, os, t, e);
+        s = t;
+        c = __fadd_rn(c, __fadd_rn(oc, e));
+    }
+    __device__ __forceinline__ float value() const { return __fadd_rn(s, c); }
+};
+
+__device__ __forceinline__ void warp_merge_kahan(Kahan& k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        float os = __shfl_xor_sync(0xffffffffu, k.s, o);
+        float oc = __shfl_xor_sync(0xffffffffu, k.c, o);
+        k.merge(os, oc);
+    }
+}
+
+__device__ __forceinline__ double warp_sum_f64(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+constexpr int kSMs = 152;
+
+inline unsigned grid_for(size_t work, unsigned per_block, unsigned cap = 1u << 20) {
+    size_t b = (work + per_block - 1) / per_block;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (unsigned)b;
+}
+
+}  // namespace gtc

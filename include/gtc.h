@@ -1,0 +1,212 @@
+/*
+ * gtc.h -- C ABI of libgtc, a GB300 (sm_103a) implementation of
+ * graph-tool-rs's centrality power iteration.
+ *
+ * The entry points replace, one for one, the Rust functions of the reference
+ * project's gt-algo crate (paths below are inside that project):
+ *
+ *   gtc_pagerank     pagerank / pagerank_with    crates/gt-algo/src/centrality.rs:234-248, 261-384
+ *   gtc_eigenvector  eigenvector                 crates/gt-algo/src/centrality.rs:405-497
+ *
+ * and the graph they run over is the reference's adjacency storage,
+ * crates/gt-core/src/adj/list.rs:67-79 (AdjList) with its per-vertex blocks
+ * crates/gt-core/src/adj/block.rs:54-57: a handle built by replaying
+ * AdjList::add_edge (list.rs:258-280) over an edge list reproduces every
+ * block's out-half and in-half order exactly, so the pull visits in-edges in
+ * the order the reference's `in_edges` yields them (crates/gt-core/src/graph.rs:228-237,
+ * crates/gt-core/src/adj/list.rs:156-161).
+ *
+ * Conventions
+ *   - Every function returns a gtc_status; on failure gtc_last_error() holds
+ *     a message for the calling thread.  Nothing aborts the process.  Error
+ *     classes follow the reference's Python boundary
+ *     (crates/gt-py/src/module.rs:78-114): GTC_ERR_ARG -> ValueError,
+ *     GTC_ERR_INDEX -> IndexError, the rest -> RuntimeError/MemoryError.
+ *   - Vertex and edge indices are uint32 (the reference's Raw = u32,
+ *     crates/gt-core/src/ids.rs:25-32).
+ *   - "Host" pointers are ordinary CPU memory; they may be pageable or
+ *     pinned.  Calls are synchronous with respect to host buffers.
+ *   - A handle is not thread-safe; use one handle per thread or lock.
+ *   - No entry point falls back to the CPU: without a usable CUDA device
+ *     they return GTC_ERR_NO_DEVICE.
+ */
+#ifndef GTC_H
+#define GTC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gtc_status {
+    GTC_OK = 0,
+    GTC_ERR_ARG = 1,       /* invalid argument (ValueError)                       */
+    GTC_ERR_OOM = 2,       /* device or host allocation failed (MemoryError)      */
+    GTC_ERR_CUDA = 3,      /* a CUDA call failed (RuntimeError)                   */
+    GTC_ERR_TIMEOUT = 4,   /* a bounded device-side wait gave up (RuntimeError)   */
+    GTC_ERR_INDEX = 5,     /* an index outside its bound (IndexError)             */
+    GTC_ERR_NO_DEVICE = 6  /* no CUDA device is usable (RuntimeError)             */
+} gtc_status;
+
+/* Arithmetic of a solve.
+ *   GTC_PREC_F32        FP32 vectors and edge weights, compensated FP32 row
+ *                       sums, FP64 dangling mass, L1 delta and
+ *                       normalisation (the fast path).
+ *   GTC_PREC_F64_EXACT  FP64 throughout with the reference's evaluation and
+ *                       fold order (per-edge divide, Plan-chunk folds): the
+ *                       result and the sweep count are bit-identical to the
+ *                       reference's for the same Plan. */
+typedef enum gtc_precision { GTC_PREC_F32 = 0, GTC_PREC_F64_EXACT = 1 } gtc_precision;
+
+typedef struct gtc_graph gtc_graph;
+
+/* PowerIteration, crates/gt-algo/src/centrality.rs:79-99.
+ *   plan_len    must equal the vertex bound (else GTC_ERR_ARG with the
+ *               reference's panic message "sweep: the plan must cover the
+ *               output exactly", centrality.rs:145-149)
+ *   plan_chunks Plan::chunks() of the caller's Plan (plan.rs:55-61); it fixes
+ *               the FP64 fold order of GTC_PREC_F64_EXACT.  0 means
+ *               Plan::new(plan_len, 4096). */
+typedef struct gtc_power_iteration {
+    double epsilon;       /* L1 change below which the sweeps stop          */
+    uint64_t max_iter;    /* hard cap on sweeps; 0 = no cap                 */
+    uint64_t plan_len;
+    uint64_t plan_chunks;
+} gtc_power_iteration;
+
+/* The directed view a solve runs on (dispatch_bidi,
+ * crates/gt-py/src/dispatch.rs:315-339): the graph, its reversal (Rev,
+ * crates/gt-core/src/view/reversed.rs:109-138), and either of them filtered
+ * by two host uint8 masks (Filtered with MaskFilter,
+ * crates/gt-core/src/view/filtered.rs:299-319): non-zero keeps.  An incident
+ * edge survives iff its edge and its other endpoint survive.  A NULL view
+ * pointer is the unfiltered graph. */
+typedef struct gtc_view {
+    int32_t reversed;
+    int32_t reserved;
+    const uint8_t* vmask;  /* NULL or length == vertex bound */
+    uint64_t vmask_len;
+    const uint8_t* emask;  /* NULL or length == edge bound   */
+    uint64_t emask_len;
+} gtc_view;
+
+/* Per-call options.  A NULL pointer means all defaults. */
+typedef struct gtc_options {
+    int32_t precision;  /* gtc_precision, default GTC_PREC_F32             */
+    int32_t schedule;   /* 0 = autotuned; otherwise a fixed unit size       */
+    void* stream;       /* cudaStream_t to run on; NULL = the handle's     */
+    int32_t timing;     /* non-zero: time every sweep kernel (sweep_ms)    */
+    int32_t reserved;
+} gtc_options;
+
+/* What a solve reports back. */
+typedef struct gtc_result {
+    uint64_t iterations;   /* sweeps performed (the reference's return)    */
+    double last_delta;     /* L1 change of the last sweep                   */
+    double eigenvalue;     /* eigenvector only: the last norm (0 if none)   */
+    double device_ms;      /* device time from the first to the last sweep  */
+    uint64_t launches;     /* kernels launched by this call                 */
+    double sweep_ms;       /* with opt->timing: summed sweep-kernel time    */
+    uint64_t sweep_launches; /* sweep kernels launched (the timed ones)     */
+} gtc_result;
+
+/* A vector in device memory (device variants of the entry points). */
+typedef enum gtc_dtype { GTC_F64 = 0, GTC_F32 = 1 } gtc_dtype;
+typedef struct gtc_dvec {
+    void* ptr;        /* device pointer (NULL: absent)                   */
+    uint64_t len;     /* elements                                        */
+    int32_t dtype;    /* gtc_dtype                                       */
+    int32_t reserved;
+} gtc_dvec;
+
+/* ---- library ---------------------------------------------------------- */
+
+const char* gtc_version(void);
+/* Message of the last failure on the calling thread ("" if none). */
+const char* gtc_last_error(void);
+
+/* ---- graphs ----------------------------------------------------------- */
+
+/* Build a graph of n vertices by replaying AdjList::add_edge(src[k], tgt[k])
+ * for k = 0..m-1 (crates/gt-core/src/adj/list.rs:258-280): edge k gets
+ * EdgeId k (alloc.rs:58-71, no removals), every out-half keeps insertion
+ * order and every in-half the push-swap rotation order of
+ * crates/gt-core/src/adj/block.rs:171-209.  Host arrays.  Replaces building
+ * an AdjList with AdjList::with_vertices + add_edge (or ParBuilder,
+ * crates/gt-core/src/adj/builder.rs:143-197, whose merge is the same call
+ * sequence). */
+int gtc_graph_create(uint64_t n, uint64_t m, const uint32_t* src, const uint32_t* tgt,
+                     gtc_graph** out);
+
+/* As gtc_graph_create, with src/tgt in device memory of the current device;
+ * `stream` (a cudaStream_t, may be NULL) orders the reads. */
+int gtc_graph_create_device(uint64_t n, uint64_t m, const uint32_t* d_src,
+                            const uint32_t* d_tgt, void* stream, gtc_graph** out);
+
+int gtc_graph_destroy(gtc_graph* g);
+
+/* Vertex bound, edge bound (AdjList::vertex_bound / edge_bound,
+ * crates/gt-core/src/graph.rs:63-67) and live edge count. */
+int gtc_graph_info(const gtc_graph* g, uint64_t* n, uint64_t* edge_bound, uint64_t* num_edges);
+
+/* Copy the blocks back to host memory: for every vertex its out-half
+ * (other, idx) entries (Block::out, block.rs:99-102) and its in-half
+ * (Block::inc, block.rs:108-111), in storage order, with n+1 offsets each.
+ * Any pointer may be NULL to skip that array. */
+int gtc_graph_export(const gtc_graph* g, uint64_t* out_off, uint32_t* out_other,
+                     uint32_t* out_idx, uint64_t* in_off, uint32_t* in_other, uint32_t* in_idx);
+
+/* Stream the handle's work is ordered on (a cudaStream_t; NULL restores the
+ * handle's own stream). */
+int gtc_graph_set_stream(gtc_graph* g, void* stream);
+
+/* ---- centrality ------------------------------------------------------- */
+
+/* PageRank: pagerank (pers == NULL) and pagerank_with (pers != NULL),
+ * crates/gt-algo/src/centrality.rs:234-384.
+ *
+ *   weight     NULL = Unity (deg = out_degree); else f64 by EdgeId, length
+ *              >= edge bound (DenseProp<f64, EdgeTag> after sized_for)
+ *   pers       NULL = Constant(1/num_vertices of the view); else f64 by
+ *              vertex index, length >= vertex bound.  Not normalised.
+ *   damping    d in nv = (1-d)*pv + d*r
+ *   rank       the caller's vertex map, length rank_len >= vertex bound: the
+ *              initial iterate AND the output.  Slots [rank_had, n) are
+ *              seeded with pers (seed_new_slots, centrality.rs:198-205), the
+ *              slots below rank_had are a warm start (sized_for,
+ *              crates/gt-core/src/prop/dense.rs:88-125).
+ *   result     iterations = the reference's return value.
+ * All arrays are host memory. */
+int gtc_pagerank(gtc_graph* g, const gtc_view* view, const double* weight, uint64_t weight_len,
+                 const double* pers, uint64_t pers_len, double damping,
+                 const gtc_power_iteration* params, double* rank, uint64_t rank_len,
+                 uint64_t rank_had, const gtc_options* opt, gtc_result* result);
+
+/* Eigenvector centrality, crates/gt-algo/src/centrality.rs:405-497.
+ * x is the initial iterate and the output (slots [x_had, n) seeded with
+ * 1/num_vertices); result->eigenvalue is the last norm, 0 if no sweep ran.
+ * All arrays are host memory. */
+int gtc_eigenvector(gtc_graph* g, const gtc_view* view, const double* weight,
+                    uint64_t weight_len, const gtc_power_iteration* params, double* x,
+                    uint64_t x_len, uint64_t x_had, const gtc_options* opt, gtc_result* result);
+
+/* Device variants: the same solves with every vector in device memory of
+ * the handle's device (e.g. torch tensors), FP32 or FP64.  NULL or ptr ==
+ * NULL means absent (Unity weights / uniform pers).  rank / x must be
+ * present.  Nothing is copied to or from the host. */
+int gtc_pagerank_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* weight,
+                        const gtc_dvec* pers, double damping, const gtc_power_iteration* params,
+                        gtc_dvec* rank, uint64_t rank_had, const gtc_options* opt,
+                        gtc_result* result);
+
+int gtc_eigenvector_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* weight,
+                           const gtc_power_iteration* params, gtc_dvec* x, uint64_t x_had,
+                           const gtc_options* opt, gtc_result* result);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GTC_H */

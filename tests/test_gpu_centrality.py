@@ -1,0 +1,191 @@
+"""PageRank and eigenvector centrality on the GPU against the oracle.
+
+* GTC_PREC_F64_EXACT: bit-identical results and sweep counts (the
+  reference's arithmetic and fold order, same Plan).
+* GTC_PREC_F32: the reference's known answers to FP32 accuracy, and
+  relative L1 error <= 1e-6 against the oracle's f64 result (the north-star
+  tolerance), with both sweep counts reported.
+"""
+import numpy as np
+import pytest
+
+import _cases as K
+
+pytestmark = pytest.mark.gpu
+
+PRECISIONS = ["f64_exact", "f32"]
+
+
+@pytest.fixture(scope="module")
+def thousand():
+    from graph_tool import synth
+    return synth.thousand()
+
+
+@pytest.fixture(scope="module")
+def eigen60():
+    from graph_tool import synth
+    return synth.eigen60()
+
+
+@pytest.fixture(scope="module")
+def er10k():
+    from graph_tool import synth
+    n, src, tgt, _ = synth.erdos_renyi_sinks()
+    return n, src, tgt
+
+
+@pytest.fixture(params=PRECISIONS)
+def S(request, gtc):
+    return K.GpuSolver(gtc, request.param)
+
+
+def test_odd_sweep_pagerank(S):
+    K.case_odd_sweep_pagerank(S)
+
+
+def test_warm_start(S):
+    K.case_warm_start(S)
+
+
+def test_cycle_and_personalisation(S):
+    K.case_cycle_and_pers(S)
+
+
+def test_zero_weight_predecessor(S):
+    K.case_zero_weight_predecessor(S)
+
+
+def test_plan_must_cover(S):
+    K.case_plan_must_cover(S)
+
+
+def test_dense_thousand(S, thousand):
+    K.case_dense_thousand(S, thousand)
+
+
+def test_cycle7_eigen(S):
+    K.case_cycle7_eigen(S)
+
+
+def test_edgeless_eigen(S):
+    K.case_edgeless_eigen(S)
+
+
+def test_odd_sweep_eigen(S):
+    K.case_odd_sweep_eigen(S)
+
+
+def test_eigen60_equation(S, eigen60):
+    K.case_eigen60(S, eigen60)
+
+
+def test_unity_is_the_general_path(S, thousand):
+    K.case_unity_is_general(S, thousand)
+
+
+# ---- bit-identity of the exact path ---------------------------------------
+
+def _variants(n, m, rng):
+    w = rng.uniform(0.1, 1.0, m)
+    w[rng.random(m) < 0.02] = 0.0      # zero weights (defect 2)
+    pers = rng.uniform(0.0, 2.0, n)     # not normalised, as the reference allows
+    vmask = (rng.random(n) < 0.9).astype(np.uint8)
+    emask = (rng.random(m) < 0.9).astype(np.uint8)
+    return [
+        dict(),
+        dict(weight=w),
+        dict(pers=pers),
+        dict(weight=w, pers=pers, reversed=True),
+        dict(vmask=vmask),
+        dict(emask=emask, weight=w),
+        dict(vmask=vmask, emask=emask, reversed=True),
+    ]
+
+
+@pytest.mark.parametrize("grain", [64, 1000, 4096])
+def test_exact_pagerank_is_bit_identical(oracle, gtc, thousand, grain):
+    n, src, tgt = thousand
+    rng = np.random.default_rng(grain)
+    O = K.OracleSolver(oracle)
+    G = K.GpuSolver(gtc, "f64_exact")
+    for kw in _variants(n, src.size, rng):
+        a, ia = O.pagerank(n, src, tgt, grain=grain, epsilon=1e-12, max_iter=500, **kw)
+        b, ib = G.pagerank(n, src, tgt, grain=grain, epsilon=1e-12, max_iter=500, **kw)
+        assert ia == ib, (kw.keys(), ia, ib)
+        assert a.tobytes() == b.tobytes(), (kw.keys(), np.max(np.abs(a - b)))
+
+
+def test_exact_pagerank_warm_start_and_cap(oracle, gtc, er10k):
+    n, src, tgt = er10k
+    O = K.OracleSolver(oracle)
+    G = K.GpuSolver(gtc, "f64_exact")
+    start = np.random.default_rng(0).uniform(0, 2.0 / n, n // 2)
+    for max_iter in (1, 2, 7):
+        a, ia = O.pagerank(n, src, tgt, grain=4096, rank=start, epsilon=1e-9, max_iter=max_iter)
+        b, ib = G.pagerank(n, src, tgt, grain=4096, rank=start, epsilon=1e-9, max_iter=max_iter)
+        assert ia == ib == max_iter
+        assert a.tobytes() == b.tobytes()
+
+
+@pytest.mark.parametrize("grain", [64, 4096])
+def test_exact_eigenvector_is_bit_identical(oracle, gtc, thousand, grain):
+    n, src, tgt = thousand
+    rng = np.random.default_rng(grain + 1)
+    O = K.OracleSolver(oracle)
+    G = K.GpuSolver(gtc, "f64_exact")
+    for kw in _variants(n, src.size, rng):
+        kw.pop("pers", None)
+        a, ea, ia = O.eigenvector(n, src, tgt, grain=grain, epsilon=1e-10, max_iter=300, **kw)
+        b, eb, ib = G.eigenvector(n, src, tgt, grain=grain, epsilon=1e-10, max_iter=300, **kw)
+        assert ia == ib and ea == eb, (kw.keys(), ia, ib, ea, eb)
+        assert a.tobytes() == b.tobytes(), kw.keys()
+
+
+# ---- FP32 against the f64 oracle -------------------------------------------
+
+def _rel_l1(a, b):
+    return float(np.abs(a - b).sum() / np.abs(b).sum())
+
+
+def test_f32_pagerank_er10k(oracle, gtc, er10k):
+    """The plain-PageRank workload (ER, n=10k, m=100k before the 5% sinks
+    lose their out-edges; d=0.85, eps=1e-6, max_iter=1000)."""
+    n, src, tgt = er10k
+    want, iw = K.OracleSolver(oracle).pagerank(n, src, tgt, grain=4096, epsilon=1e-6,
+                                               max_iter=1000)
+    got, ig = K.GpuSolver(gtc, "f32").pagerank(n, src, tgt, grain=4096, epsilon=1e-6,
+                                               max_iter=1000)
+    err = _rel_l1(got, want)
+    print(f"ER10k f32: rel L1 {err:.3e}, max abs {np.max(np.abs(got - want)):.3e}, "
+          f"sweeps gpu {ig} oracle {iw}")
+    assert err < 1e-6
+    assert abs(ig - iw) <= 2
+
+
+def test_f32_variants_rel_l1(oracle, gtc, thousand):
+    n, src, tgt = thousand
+    rng = np.random.default_rng(11)
+    for kw in _variants(n, src.size, rng):
+        want, iw = K.OracleSolver(oracle).pagerank(n, src, tgt, grain=64, epsilon=1e-7,
+                                                   max_iter=2000, **kw)
+        got, ig = K.GpuSolver(gtc, "f32").pagerank(n, src, tgt, grain=64, epsilon=1e-7,
+                                                   max_iter=2000, **kw)
+        active = np.ones(n, bool) if "vmask" not in kw else kw["vmask"].astype(bool)
+        err = _rel_l1(got[active], want[active])
+        assert err < 1e-6, (kw.keys(), err, ig, iw)
+        # inactive slots carry the initial iterate through unchanged
+        assert np.array_equal(got[~active], want[~active])
+
+
+def test_f32_eigenvector_rel_l1(oracle, gtc, er10k):
+    n, src, tgt = er10k
+    w = np.random.default_rng(5).uniform(0.1, 1.0, src.size)
+    want, ew, iw = K.OracleSolver(oracle).eigenvector(n, src, tgt, weight=w, grain=4096,
+                                                      epsilon=1e-7, max_iter=500)
+    got, eg, ig = K.GpuSolver(gtc, "f32").eigenvector(n, src, tgt, weight=w, grain=4096,
+                                                      epsilon=1e-7, max_iter=500)
+    err = _rel_l1(got, want)
+    print(f"eigen f32: rel L1 {err:.3e}, eig {eg} vs {ew}, sweeps {ig} vs {iw}")
+    assert err < 1e-5
+    assert abs(eg - ew) / ew < 1e-6
