@@ -54,6 +54,8 @@ WORKLOADS = {
     "chunglu": dict(gen="chunglu", n=4_194_304, m=67_108_864, seed=2, weighted=True, eps=1e-7,
                     label="Chung-Lu n=4,194,304 m~67M, Pareto(2.1, min 2, cap 1e5) "
                           "degrees, FP32 weights U(0.1,1), weighted"),
+    "rmat22": dict(gen="rmat", scale=22, edge_factor=16, seed=1, weighted=False, eps=1e-7,
+                   label="R-MAT scale 22, edge factor 16 (profiling size, > L2)"),
     "rmat20": dict(gen="rmat", scale=20, edge_factor=16, seed=1, weighted=False, eps=1e-7,
                    label="R-MAT scale 20, edge factor 16 (small test size)"),
 }
@@ -144,8 +146,10 @@ def make_graph(wl, device, rank):
     else:
         n, src, tgt, w = synth_gpu.chung_lu(wl["n"], wl["m"], seed=wl["seed"] + rank,
                                             device=device)
+    src, tgt = src.contiguous(), tgt.contiguous()
     torch.cuda.synchronize()
-    return n, src.contiguous(), tgt.contiguous(), w
+    torch.cuda.empty_cache()
+    return n, src, tgt, w
 
 
 def algorithmic_bytes(n, m, weighted, pers=False):

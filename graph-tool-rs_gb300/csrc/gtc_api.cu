@@ -160,26 +160,33 @@ int gtc_graph_export(const gtc_graph* g, uint64_t* out_off, uint32_t* out_other,
     return guarded([&] {
         GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
         cudaStream_t s = g->home;
-        const size_t n1 = (size_t)g->n + 1, m = g->m;
-        std::vector<uint32_t> tmp(n1);
-        auto offs = [&](const DevBuf<uint32_t>& d, uint64_t* h) {
-            if (!h) return;
-            GTC_CUDA(cudaMemcpyAsync(tmp.data(), d.get(), n1 * sizeof(uint32_t),
-                                     cudaMemcpyDeviceToHost, s));
-            GTC_CUDA(cudaStreamSynchronize(s));
-            for (size_t i = 0; i < n1; ++i) h[i] = tmp[i];
-        };
-        auto arr = [&](const DevBuf<uint32_t>& d, uint32_t* h) {
-            if (h && m)
-                GTC_CUDA(cudaMemcpyAsync(h, d.get(), m * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        };
-        offs(g->out.off, out_off);
-        offs(g->in.off, in_off);
-        arr(g->out.other, out_other);
-        arr(g->out.eid, out_idx);
-        arr(g->in.other, in_other);
-        arr(g->in.eid, in_idx);
+        const size_t n = g->n, m = g->m;
+        std::vector<uint32_t> perm(n), iperm(n), off(n + 1), other(m), eid(m);
+        if (n) GTC_CUDA(cudaMemcpyAsync(perm.data(), g->perm.get(), n * 4, cudaMemcpyDeviceToHost, s));
         GTC_CUDA(cudaStreamSynchronize(s));
+        for (size_t i = 0; i < n; ++i) iperm[perm[i]] = (uint32_t)i;
+        // one half, back in original labels and original block order
+        auto half = [&](const Halves& h, uint64_t* hoff, uint32_t* hother, uint32_t* hidx) {
+            if (!hoff && !hother && !hidx) return;
+            GTC_CUDA(cudaMemcpyAsync(off.data(), h.off.get(), (n + 1) * 4, cudaMemcpyDeviceToHost, s));
+            if (m) {
+                GTC_CUDA(cudaMemcpyAsync(other.data(), h.other.get(), m * 4, cudaMemcpyDeviceToHost, s));
+                GTC_CUDA(cudaMemcpyAsync(eid.data(), h.eid.get(), m * 4, cudaMemcpyDeviceToHost, s));
+            }
+            GTC_CUDA(cudaStreamSynchronize(s));
+            uint64_t pos = 0;
+            for (size_t v = 0; v < n; ++v) {
+                if (hoff) hoff[v] = pos;
+                const uint32_t i = iperm[v];
+                for (uint32_t p = off[i]; p < off[i + 1]; ++p, ++pos) {
+                    if (hother) hother[pos] = perm[other[p]];
+                    if (hidx) hidx[pos] = eid[p];
+                }
+            }
+            if (hoff) hoff[n] = pos;
+        };
+        half(g->out, out_off, out_other, out_idx);
+        half(g->in, in_off, in_other, in_idx);
     });
 }
 

@@ -360,6 +360,83 @@ __global__ void k_fix_place(uint32_t m, const uint32_t* __restrict__ rowkey,
         atomicOr(bad, 2u);
 }
 
+// --------------------------------------------------------------------------
+// relabelling by descending out-degree
+// --------------------------------------------------------------------------
+
+__global__ void k_degree_key(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ deg,
+                             unsigned* __restrict__ maxdeg) {
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t d = v < n ? off[v + 1] - off[v] : 0u;
+    if (v < n) deg[v] = d;
+    // warp max, one atomic per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d = max(d, __shfl_xor_sync(0xffffffffu, d, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxdeg, d);
+}
+
+__global__ void k_desc_key(uint32_t n, const uint32_t* __restrict__ deg, uint32_t maxdeg,
+                           uint32_t* __restrict__ key) {
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) key[v] = maxdeg - deg[v];
+}
+
+__global__ void k_invert(uint32_t n, const uint32_t* __restrict__ perm, uint32_t* __restrict__ iperm) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) iperm[perm[i]] = (uint32_t)i;
+}
+
+__global__ void k_new_degrees(uint32_t n, const uint32_t* __restrict__ perm,
+                              const uint32_t* __restrict__ off, uint32_t* __restrict__ deg) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) deg[i] = off[perm[i] + 1] - off[perm[i]];
+}
+
+// One warp per new row: copy the old block half in order, relabelling the
+// other endpoint (looked up by edge id in the original edge list).
+__global__ void k_permute_rows(uint32_t n, const uint32_t* __restrict__ perm,
+                               const uint32_t* __restrict__ iperm,
+                               const uint32_t* __restrict__ old_off,
+                               const uint32_t* __restrict__ old_eid,
+                               const uint32_t* __restrict__ endpoint,
+                               const uint32_t* __restrict__ new_off, uint32_t* __restrict__ new_eid,
+                               uint32_t* __restrict__ new_other) {
+    const unsigned lane = threadIdx.x & 31;
+    const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t i = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nw) {
+        const uint32_t v = perm[i];
+        const uint32_t b = old_off[v], e = old_off[v + 1], nb = new_off[i];
+        for (uint32_t p = b + lane; p < e; p += 32) {
+            const uint32_t id = old_eid[p];
+            new_eid[nb + (p - b)] = id;
+            new_other[nb + (p - b)] = iperm[endpoint[id]];
+        }
+    }
+}
+
+static void relabel_half(uint32_t n, uint32_t m, const uint32_t* perm, const uint32_t* iperm,
+                         const uint32_t* endpoint, Halves& h, cudaStream_t s, uint64_t* L) {
+    const unsigned TB = 256;
+    Halves nh;
+    nh.off.alloc((size_t)n + 1, s);
+    nh.eid.alloc(m, s);
+    nh.other.alloc(m, s);
+    DevBuf<uint32_t> deg(n, s);
+    if (n) {
+        k_new_degrees<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, perm, h.off.get(), deg.get());
+        GTC_LAUNCHED();
+        *L += 1;
+    }
+    scan_exclusive_u32(deg.get(), nh.off.get(), n, s, L);
+    if (n && m) {
+        k_permute_rows<<<kSMs * 16, TB, 0, s>>>(n, perm, iperm, h.off.get(), h.eid.get(), endpoint,
+                                               nh.off.get(), nh.eid.get(), nh.other.get());
+        GTC_LAUNCHED();
+        *L += 1;
+    }
+    h = std::move(nh);
+}
+
 void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt) {
     cudaStream_t s = g->home;
     const uint32_t n = g->n, m = g->m;
@@ -394,12 +471,6 @@ void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt) {
                                                                             g->out.off.get());
     GTC_LAUNCHED();
     L += 1;
-    if (m > 0) {
-        k_gather_u32<<<grid_for(m, TB, 1u << 30), TB, 0, s>>>(g->out.eid.get(), d_tgt,
-                                                             g->out.other.get(), m);
-        GTC_LAUNCHED();
-        L += 1;
-    }
 
     // in-halves: stable by target (push order), then the rotation
     DevBuf<uint32_t> in_sorted(m, s);
@@ -423,10 +494,30 @@ void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt) {
         GTC_CUDA(cudaMemcpyAsync(&hbad, bad.get(), sizeof(unsigned), cudaMemcpyDeviceToHost, s));
         GTC_CUDA(cudaStreamSynchronize(s));
         GTC_REQUIRE(!hbad, GTC_ERR_CUDA, "in-half placement left its segment (internal error)");
-        k_gather_u32<<<gb, TB, 0, s>>>(g->in.eid.get(), d_src, g->in.other.get(), m);
+        L += 2;
+    }
+
+    // relabel by descending out-degree (stable: ties keep index order)
+    g->perm.alloc(n, s);
+    g->iperm.alloc(n, s);
+    if (n) {
+        DevBuf<uint32_t> deg(n, s), key(n, s), skey(n, s);
+        DevBuf<unsigned> mx(1, s);
+        GTC_CUDA(cudaMemsetAsync(mx.get(), 0, sizeof(unsigned), s));
+        k_degree_key<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->out.off.get(), deg.get(), mx.get());
+        GTC_LAUNCHED();
+        unsigned maxdeg = 0;
+        GTC_CUDA(cudaMemcpyAsync(&maxdeg, mx.get(), sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+        k_desc_key<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, deg.get(), maxdeg, key.get());
+        GTC_LAUNCHED();
+        sort_positions_by_key(key.get(), n, maxdeg + 1, skey.get(), g->perm.get(), s, &L);
+        k_invert<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->perm.get(), g->iperm.get());
         GTC_LAUNCHED();
         L += 3;
     }
+    relabel_half(n, m, g->perm.get(), g->iperm.get(), d_tgt, g->out, s, &L);
+    relabel_half(n, m, g->perm.get(), g->iperm.get(), d_src, g->in, s, &L);
     GTC_CUDA(cudaStreamSynchronize(s));
     g->launches += L;
 }

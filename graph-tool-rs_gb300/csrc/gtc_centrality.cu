@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "gtc_sweep.cuh"
 #include "gtc_view.cuh"
 
 namespace gtc {
@@ -74,69 +75,7 @@ __device__ __forceinline__ void block_fold2(double a, double b, const Fold2& f) 
     }
 }
 
-// --------------------------------------------------------------------------
-// FP32 PageRank
-// --------------------------------------------------------------------------
-
-struct PrF32 {
-    uint32_t n;
-    const uint32_t* __restrict__ off;    // pull offsets (n+1)
-    const uint32_t* __restrict__ other;  // pull sources
-    const float* __restrict__ w;         // pull-ordered weights or null
-    const float* __restrict__ invdeg;    // 1/deg, 0 for sinks and inactive
-    const uint8_t* __restrict__ sink;    // active && deg == 0
-    const uint8_t* __restrict__ active;  // null = all
-    const float* __restrict__ pers;      // null = uniform
-    float uniform;
-    float one_minus_d, d;
-    const double* psink;  // dangling mass of prev
-    const float* __restrict__ prev;
-    const float* __restrict__ yprev;
-    float* __restrict__ next;
-    float* __restrict__ ynext;
-    Fold2 fold;  // a = delta, b = dangling mass of next
-};
-
 constexpr int PR_NT = 256;
-
-// One warp per row (grid-stride).  Lanes stride the row's in-edges with a
-// compensated sum, merged across the warp with TwoSum.
-template <bool WEIGHTED>
-__global__ void __launch_bounds__(PR_NT) k_pr_f32_warp(PrF32 a) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t gw = (blockIdx.x * PR_NT + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * PR_NT) >> 5;
-    const float psink = (float)*a.psink;
-    Kahan dacc, sacc;
-    for (uint32_t row = gw; row < a.n; row += nw) {
-        if (a.active && !a.active[row]) {
-            if (lane == 0) {
-                a.next[row] = a.prev[row];
-                a.ynext[row] = 0.f;
-            }
-            continue;
-        }
-        const uint32_t b = a.off[row], e = a.off[row + 1];
-        Kahan k;
-        for (uint32_t p = b + lane; p < e; p += 32) {
-            float x = a.yprev[a.other[p]];
-            if (WEIGHTED) x = __fmul_rn(x, a.w[p]);
-            k.add(x);
-        }
-        warp_merge_kahan(k);
-        if (lane == 0) {
-            const float pv = a.pers ? a.pers[row] : a.uniform;
-            const float r = __fadd_rn(__fmul_rn(psink, pv), k.value());
-            const float nv = __fadd_rn(__fmul_rn(a.one_minus_d, pv), __fmul_rn(a.d, r));
-            const float pr = a.prev[row];
-            a.next[row] = nv;
-            a.ynext[row] = __fmul_rn(nv, a.invdeg[row]);
-            dacc.add(fabsf(__fsub_rn(nv, pr)));
-            if (a.sink[row]) sacc.add(nv);
-        }
-    }
-    block_fold2<PR_NT>((double)dacc.s + (double)dacc.c, (double)sacc.s + (double)sacc.c, a.fold);
-}
 
 // --------------------------------------------------------------------------
 // per-call preparation kernels
@@ -177,30 +116,40 @@ __global__ void k_gather_w(uint32_t m, const uint32_t* __restrict__ eid,
     if (p < m) out[p] = (T)ld_any(w, wdt, eid[p]);
 }
 
-// Initial iterate (FP64): slots below `had` come from the caller's map, the
-// rest are seeded (seed_new_slots, centrality.rs:198-205).
-__global__ void k_seed(uint32_t n, uint64_t had, const void* __restrict__ x, int xdt,
-                       const void* __restrict__ pers, int pdt, double uniform,
-                       double* __restrict__ x64) {
-    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n) return;
-    x64[v] = v < had ? ld_any(x, xdt, v) : (pers ? ld_any(pers, pdt, v) : uniform);
+// Initial iterate (FP64, internal labels): slots below `had` come from the
+// caller's map, the rest are seeded (seed_new_slots, centrality.rs:198-205).
+// The caller's maps are by original index: internal slot i is vertex perm[i].
+__global__ void k_seed(uint32_t n, const uint32_t* __restrict__ perm, uint64_t had,
+                       const void* __restrict__ x, int xdt, const void* __restrict__ pers, int pdt,
+                       double uniform, double* __restrict__ x64) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t v = perm[i];
+    x64[i] = v < had ? ld_any(x, xdt, v) : (pers ? ld_any(pers, pdt, v) : uniform);
 }
 
-__global__ void k_to_f32(uint32_t n, const void* __restrict__ x, int xdt, float* __restrict__ y) {
-    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v < n) y[v] = (float)ld_any(x, xdt, v);
+// FP32 copy; with `perm` the source is in original labels.
+__global__ void k_to_f32(uint32_t n, const void* __restrict__ x, int xdt,
+                         const uint32_t* __restrict__ perm, float* __restrict__ y) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = (float)ld_any(x, xdt, perm ? perm[i] : i);
 }
 
-// Store an iterate into the caller's map, in the map's type.
+// Store an iterate into the caller's map, in the map's type.  Slots of
+// vertices outside a filtered view keep their FP64 initial value exactly (the
+// reference carries them through untouched, centrality.rs:345-351).
 template <class T>
-__global__ void k_store(uint32_t n, const T* __restrict__ src, void* __restrict__ x, int xdt) {
+__global__ void k_store(uint32_t n, const uint32_t* __restrict__ iperm, const T* __restrict__ src,
+                        const uint8_t* __restrict__ active, const double* __restrict__ x64,
+                        void* __restrict__ x, int xdt) {
     size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
+    const uint32_t i = iperm[v];
+    const double val = (active && !active[i]) ? x64[i] : (double)src[i];
     if (xdt == GTC_F64)
-        ((double*)x)[v] = (double)src[v];
+        ((double*)x)[v] = val;
     else
-        ((float*)x)[v] = (float)src[v];
+        ((float*)x)[v] = (float)val;
 }
 
 // y = rank * invdeg, plus the dangling mass of rank (block-folded).
@@ -288,15 +237,20 @@ __global__ void k_fold(uint64_t chunks, const double* __restrict__ part, double*
     }
 }
 
-__global__ void k_compact_sinks(uint32_t n, const uint8_t* __restrict__ sink,
+// The sinks in original vertex order (the reference's `sinks` list,
+// centrality.rs:281-297), as internal labels for gathering.
+__global__ void k_compact_sinks(uint32_t n, const uint32_t* __restrict__ flag,
+                                const uint32_t* __restrict__ iperm,
                                 const uint32_t* __restrict__ pos, uint32_t* __restrict__ list) {
     size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v < n && sink[v]) list[pos[v]] = (uint32_t)v;
+    if (v < n && flag[v]) list[pos[v]] = iperm[v];
 }
 
-__global__ void k_u8_to_u32(uint32_t n, const uint8_t* __restrict__ a, uint32_t* __restrict__ b) {
+// flag[v] (original order) = sink[iperm[v]]
+__global__ void k_sink_flags(uint32_t n, const uint32_t* __restrict__ iperm,
+                             const uint8_t* __restrict__ sink, uint32_t* __restrict__ flag) {
     size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v < n) b[v] = a[v];
+    if (v < n) flag[v] = sink[iperm[v]];
 }
 
 // Eigenvector sweep 1 (centrality.rs:446-465): s = sum w*prev[other] in
@@ -340,58 +294,26 @@ __global__ void k_ev_f64_norm(uint32_t n, const uint8_t* __restrict__ active,
 // FP32 eigenvector
 // --------------------------------------------------------------------------
 
-struct EvF32 {
-    uint32_t n;
-    const uint32_t* __restrict__ off;
-    const uint32_t* __restrict__ other;
-    const float* __restrict__ w;
-    const uint8_t* __restrict__ active;
-    const float* __restrict__ prev;
-    float* __restrict__ next;
-    Fold2 fold;  // a = squared norm
-};
-
-template <bool WEIGHTED>
-__global__ void __launch_bounds__(PR_NT) k_ev_f32_warp(EvF32 a) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t gw = (blockIdx.x * PR_NT + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * PR_NT) >> 5;
-    Kahan qacc;
-    for (uint32_t row = gw; row < a.n; row += nw) {
-        if (a.active && !a.active[row]) {
-            if (lane == 0) a.next[row] = a.prev[row];
-            continue;
-        }
-        const uint32_t b = a.off[row], e = a.off[row + 1];
-        Kahan k;
-        for (uint32_t p = b + lane; p < e; p += 32) {
-            float x = a.prev[a.other[p]];
-            if (WEIGHTED) x = __fmul_rn(a.w[p], x);
-            k.add(x);
-        }
-        warp_merge_kahan(k);
-        if (lane == 0) {
-            const float s = k.value();
-            a.next[row] = s;
-            qacc.add(__fmul_rn(s, s));
-        }
-    }
-    block_fold2<PR_NT>((double)qacc.s + (double)qacc.c, 0.0, a.fold);
-}
-
 // next /= scale (scale from the FP64 norm, 1 if zero) and the FP64 delta.
+// The FP64 reciprocal is applied as an unevaluated sum hi + lo of two floats,
+// so the stored value is (nearly always) the correctly rounded s / norm: a
+// last-bit change of the norm between sweeps does not move every entry by an
+// ulp, which would put a floor of ~sqrt(n) * 2^-24 under the L1 change.
 __global__ void __launch_bounds__(PR_NT) k_ev_f32_norm(uint32_t n,
                                                       const uint8_t* __restrict__ active,
                                                       const double* __restrict__ sqnorm,
                                                       const float* __restrict__ prev,
                                                       float* __restrict__ next, Fold2 f) {
     const double norm = sqrt(*sqnorm);
-    const float inv = (float)(1.0 / (norm == 0.0 ? 1.0 : norm));
+    const double inv = 1.0 / (norm == 0.0 ? 1.0 : norm);
+    const float ih = (float)inv;
+    const float il = (float)(inv - (double)ih);
     Kahan dacc;
     for (size_t v = (size_t)blockIdx.x * PR_NT + threadIdx.x; v < n;
          v += (size_t)gridDim.x * PR_NT) {
         if (active && !active[v]) continue;
-        const float x = __fmul_rn(next[v], inv);
+        const float sv = next[v];
+        const float x = __fmaf_rn(sv, ih, __fmul_rn(sv, il));
         next[v] = x;
         dacc.add(fabsf(__fsub_rn(x, prev[v])));
     }
@@ -445,6 +367,56 @@ unsigned persistent_blocks(uint32_t rows) {
     return want < 1 ? 1 : (want > cap ? cap : want);
 }
 
+// The pull schedule of a view: cached on the graph for the plain and the
+// reversed view, cut per call for a filtered one.
+Units* pull_units(gtc_graph* g, const View& view, Units& local, cudaStream_t s) {
+    if (!view.filtered) {
+        Units& u = view.reversed ? g->units_out : g->units_in;
+        if (!u.built) {
+            GTC_CUDA(cudaStreamSynchronize(s));
+            build_units(view.pull_off, view.n, g->home, u);
+        }
+        return &u;
+    }
+    build_units(view.pull_off, view.n, s, local);
+    return &local;
+}
+
+template <int MODE, bool W>
+unsigned sweep_grid(uint32_t n_units) {
+    static int per_sm = 0, sms = 0;
+    if (!per_sm) {
+        int dev = 0;
+        GTC_CUDA(cudaGetDevice(&dev));
+        GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<MODE, W>, SP_NT, 0));
+        if (per_sm < 1) per_sm = 1;
+    }
+    const unsigned cap = (unsigned)(per_sm * sms);
+    return n_units < 1 ? 1u : (n_units < cap ? n_units : cap);
+}
+
+template <int MODE>
+void launch_sweep(const SweepArgs& A, bool weighted, unsigned nb, cudaStream_t s) {
+    if (weighted)
+        k_sweep<MODE, true><<<nb, SP_NT, 0, s>>>(A);
+    else
+        k_sweep<MODE, false><<<nb, SP_NT, 0, s>>>(A);
+    GTC_LAUNCHED();
+}
+
+void set_schedule(SweepArgs& A, const Units& u, const View& view) {
+    A.units = u.units.get();
+    A.longs = u.longs.get();
+    A.partial = u.partial.get();
+    A.counter = u.counter.get();
+    A.long_out = u.long_out.get();
+    A.n_units = u.n_units;
+    A.n_long = u.n_long;
+    A.off = view.pull_off;
+    A.other = view.pull_other;
+}
+
 // Everything a sweep loop needs that does not change between sweeps.
 struct Prep {
     View view;
@@ -473,17 +445,21 @@ void prepare(gtc_graph* g, const gtc_view* vw, const SolveIn& in, bool need_deg,
     }
     P.x64.alloc(n, s);
     if (n) {
-        k_seed<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, in.had, in.x, in.x_dtype, in.pers.p,
-                                                        in.pers.dtype, P.uniform, P.x64.get());
+        k_seed<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->perm.get(), in.had, in.x, in.x_dtype,
+                                                        in.pers.p, in.pers.dtype, P.uniform,
+                                                        P.x64.get());
         GTC_LAUNCHED();
         (*L)++;
     }
 }
 
 template <class T>
-void store_result(uint32_t n, const T* src, const SolveIn& in, cudaStream_t s, uint64_t* L) {
+void store_result(gtc_graph* g, uint32_t n, const T* src, const Prep& P, const SolveIn& in,
+                  cudaStream_t s, uint64_t* L) {
     if (!n) return;
-    k_store<T><<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, src, in.x, in.x_dtype);
+    k_store<T><<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, g->iperm.get(), src,
+                                                          P.view.active_or_null(), P.x64.get(),
+                                                          in.x, in.x_dtype);
     GTC_LAUNCHED();
     (*L)++;
 }
@@ -525,7 +501,8 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         // sinks in vertex order and their Plan (grain_of, centrality.rs:186-188, :311)
         DevBuf<uint32_t> flag32(n, s), pos((size_t)n + 1, s);
         if (n) {
-            k_u8_to_u32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.sink.get(), flag32.get());
+            k_sink_flags<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->iperm.get(), P.sink.get(),
+                                                                  flag32.get());
             GTC_LAUNCHED();
             L++;
         }
@@ -535,8 +512,8 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         GTC_CUDA(cudaStreamSynchronize(s));
         DevBuf<uint32_t> sinks(n_sinks, s);
         if (n) {
-            k_compact_sinks<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.sink.get(), pos.get(),
-                                                                     sinks.get());
+            k_compact_sinks<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, flag32.get(), g->iperm.get(),
+                                                                     pos.get(), sinks.get());
             GTC_LAUNCHED();
             L++;
         }
@@ -548,12 +525,11 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         const double* pers64 = nullptr;
         DevBuf<double> pbuf;
         if (in.pers.present()) {
-            if (in.pers.dtype == GTC_F64) {
-                pers64 = (const double*)in.pers.p;
-            } else {
+            {  // pers by internal label
                 pbuf.alloc(n, s);
-                k_seed<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, n, in.pers.p, in.pers.dtype,
-                                                                nullptr, 0, 0.0, pbuf.get());
+                k_seed<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->perm.get(), n, in.pers.p,
+                                                                in.pers.dtype, nullptr, 0, 0.0,
+                                                                pbuf.get());
                 GTC_LAUNCHED();
                 L++;
                 pers64 = pbuf.get();
@@ -571,8 +547,9 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
                 k_pr_f64_rows<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(
                     n, view.pull_off, view.pull_other, wpull.get(), P.deg.get(), act, pers64,
                     P.uniform, 1.0 - d, d, scal.get(), cur, nxt, diff.get());
+            // the delta is folded over the Plan in original vertex order
             k_chunk_sums<<<grid_for(chunks, 128, 1u << 30), 128, 0, s>>>(n, chunks, diff.get(),
-                                                                         nullptr, part.get());
+                                                                         g->iperm.get(), part.get());
             k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get() + 1, nullptr, 0);
             GTC_LAUNCHED();
             if (in.timing) sw.stop();
@@ -587,7 +564,7 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         }
         total.stop();
         res->device_ms = total.ms();
-        store_result<double>(n, cur, in, s, &L);
+        store_result<double>(g, n, cur, P, in, s, &L);
     } else {
         DevBuf<float> invdeg(n, s);
         if (n) {
@@ -600,13 +577,14 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         if (in.pers.present() && n) {
             pers32.alloc(n, s);
             k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, in.pers.p, in.pers.dtype,
-                                                              pers32.get());
+                                                              g->perm.get(), pers32.get());
             GTC_LAUNCHED();
             L++;
         }
         DevBuf<float> r0(n, s), r1(n, s), y0(n, s), y1(n, s);
         if (n) {
-            k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.x64.get(), GTC_F64, r0.get());
+            k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.x64.get(), GTC_F64, nullptr,
+                                                              r0.get());
             GTC_LAUNCHED();
             L++;
         }
@@ -618,33 +596,39 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         GTC_LAUNCHED();
         L++;
         float *rc = r0.get(), *rn = r1.get(), *yc = y0.get(), *yn = y1.get();
-        PrF32 a;
-        a.n = n;
-        a.off = view.pull_off;
-        a.other = view.pull_other;
-        a.w = wpull.get();
-        a.invdeg = invdeg.get();
-        a.sink = P.sink.get();
-        a.active = act;
-        a.pers = pers32.get();
-        a.uniform = (float)P.uniform;
-        a.one_minus_d = (float)(1.0 - d);
-        a.d = (float)d;
-        a.psink = dp + 1;
-        a.fold = fb.fold(dp + 0, dp + 1);
+        Units local;
+        const Units* U = pull_units(g, view, local, s);
+        const bool W = in.weight.present();
+        const unsigned grid = W ? sweep_grid<MODE_PAGERANK, true>(U->n_units)
+                                : sweep_grid<MODE_PAGERANK, false>(U->n_units);
+        FoldBufs fs(grid, s);
+        double* dq = fs.out.get();
+        // the dangling mass of the initial iterate seeds the first sweep
+        GTC_CUDA(cudaMemcpyAsync(dq + 1, dp + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
+        SweepArgs A{};
+        set_schedule(A, *U, view);
+        A.w = wpull.get();
+        A.active = act;
+        A.invdeg = invdeg.get();
+        A.sink = P.sink.get();
+        A.pers = pers32.get();
+        A.uniform = (float)P.uniform;
+        A.one_minus_d = (float)(1.0 - d);
+        A.d = (float)d;
+        A.psink = dq + 1;
+        A.part_a = fs.pa.get();
+        A.part_b = fs.pb.get();
+        A.ticket = fs.ticket.get();
+        A.out = dq;
         total.start();
         while (delta >= eps) {
-            a.prev = rc, a.yprev = yc, a.next = rn, a.ynext = yn;
+            A.x = yc, A.prev = rc, A.next = rn, A.ynext = yn;
             if (in.timing) sw.start();
-            if (in.weight.present())
-                k_pr_f32_warp<true><<<nb, PR_NT, 0, s>>>(a);
-            else
-                k_pr_f32_warp<false><<<nb, PR_NT, 0, s>>>(a);
-            GTC_LAUNCHED();
+            launch_sweep<MODE_PAGERANK>(A, W, grid, s);
             if (in.timing) sw.stop();
             L++;
             SL++;
-            GTC_CUDA(cudaMemcpyAsync(&delta, dp, sizeof(double), cudaMemcpyDeviceToHost, s));
+            GTC_CUDA(cudaMemcpyAsync(&delta, dq, sizeof(double), cudaMemcpyDeviceToHost, s));
             GTC_CUDA(cudaStreamSynchronize(s));
             if (in.timing) sweep_ms += sw.ms();
             std::swap(rc, rn);
@@ -654,7 +638,7 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         }
         total.stop();
         res->device_ms = total.ms();
-        store_result<float>(n, rc, in, s, &L);
+        store_result<float>(g, n, rc, P, in, s, &L);
     }
     GTC_CUDA(cudaStreamSynchronize(s));
     res->iterations = iter;
@@ -692,14 +676,14 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
                 k_ev_f64_rows<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(
                     n, view.pull_off, view.pull_other, wpull.get(), act, cur, nxt, tmp.get());
             k_chunk_sums<<<grid_for(chunks, 128, 1u << 30), 128, 0, s>>>(n, chunks, tmp.get(),
-                                                                         nullptr, part.get());
+                                                                         g->iperm.get(), part.get());
             // scal[0] = squared norm, scal[1] = norm, scal[2] = scale
             k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get(), scal.get() + 2, 1);
             if (n)
                 k_ev_f64_norm<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(n, act, scal.get() + 2,
                                                                          cur, nxt, tmp.get());
             k_chunk_sums<<<grid_for(chunks, 128, 1u << 30), 128, 0, s>>>(n, chunks, tmp.get(),
-                                                                         nullptr, part.get());
+                                                                         g->iperm.get(), part.get());
             k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get() + 3, nullptr, 0);
             GTC_LAUNCHED();
             if (in.timing) sw.stop();
@@ -717,35 +701,39 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         }
         total.stop();
         res->device_ms = total.ms();
-        store_result<double>(n, cur, in, s, &L);
+        store_result<double>(g, n, cur, P, in, s, &L);
     } else {
         DevBuf<float> wpull = pull_weights<float>(P, in, s, &L);
         DevBuf<float> x0(n, s), x1(n, s);
         if (n) {
-            k_to_f32<<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, P.x64.get(), GTC_F64, x0.get());
+            k_to_f32<<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, P.x64.get(), GTC_F64, nullptr,
+                                                                x0.get());
             GTC_LAUNCHED();
             L++;
         }
+        Units local;
+        const Units* U = pull_units(g, view, local, s);
+        const bool W = in.weight.present();
+        const unsigned grid = W ? sweep_grid<MODE_EIGEN, true>(U->n_units)
+                                : sweep_grid<MODE_EIGEN, false>(U->n_units);
         const unsigned nb = persistent_blocks(n);
-        FoldBufs f1(nb, s), f2(nb, s);
+        FoldBufs f1(grid, s), f2(nb, s);
         double* o1 = f1.out.get();
         double* o2 = f2.out.get();
         float *xc = x0.get(), *xn = x1.get();
-        EvF32 a;
-        a.n = n;
-        a.off = view.pull_off;
-        a.other = view.pull_other;
-        a.w = wpull.get();
-        a.active = act;
-        a.fold = f1.fold(o1, o1 + 1);
+        SweepArgs A{};
+        set_schedule(A, *U, view);
+        A.w = wpull.get();
+        A.active = act;
+        A.part_a = f1.pa.get();
+        A.part_b = f1.pb.get();
+        A.ticket = f1.ticket.get();
+        A.out = o1;
         total.start();
         while (delta >= eps) {
-            a.prev = xc, a.next = xn;
+            A.x = xc, A.prev = xc, A.next = xn;
             if (in.timing) sw.start();
-            if (in.weight.present())
-                k_ev_f32_warp<true><<<nb, PR_NT, 0, s>>>(a);
-            else
-                k_ev_f32_warp<false><<<nb, PR_NT, 0, s>>>(a);
+            launch_sweep<MODE_EIGEN>(A, W, grid, s);
             k_ev_f32_norm<<<nb, PR_NT, 0, s>>>(n, act, o1, xc, xn, f2.fold(o2, o2 + 1));
             GTC_LAUNCHED();
             if (in.timing) sw.stop();
@@ -763,7 +751,7 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         }
         total.stop();
         res->device_ms = total.ms();
-        store_result<float>(n, xc, in, s, &L);
+        store_result<float>(g, n, xc, P, in, s, &L);
     }
     GTC_CUDA(cudaStreamSynchronize(s));
     res->iterations = iter;

@@ -101,12 +101,16 @@ struct Halves {
     DevBuf<uint32_t> off, other, eid;
 };
 
-// Pull schedule of one direction: the rows cut into work units of about
-// equal (rows + entries), computed once per graph.
-struct Schedule {
-    DevBuf<uint2> units;  // see gtc_pagerank.cu: {row_begin, row_end|LONG_FLAG} or chunk
-    uint32_t n_units = 0;
-    uint32_t cap = 0;     // merge items per unit the schedule was cut for
+// Pull schedule of one half: its rows cut into work units of at most a
+// fixed number of merge items (rows + entries); see gtc_sweep.cuh.
+struct Units {
+    DevBuf<uint4> units;       // the work list
+    DevBuf<uint4> longs;       // per long row: {row, first chunk slot, chunks, 0}
+    DevBuf<float2> partial;    // per long chunk: compensated partial (s, c)
+    DevBuf<unsigned> counter;  // per long row: chunks done (reset by the last)
+    DevBuf<double2> long_out;  // per long row: its epilogue's reduction terms
+    uint32_t n_units = 0, n_long = 0, n_chunks = 0;
+    bool built = false;
 };
 
 }  // namespace gtc
@@ -117,9 +121,14 @@ struct gtc_graph {
     uint32_t m = 0;  // edge bound == live edges (ids 0..m-1)
     cudaStream_t home = nullptr;    // owned; graph-lifetime buffers live on it
     cudaStream_t stream = nullptr;  // where solves run (home, or the caller's)
+    // Internally vertices are relabelled by descending out-degree (ties by
+    // index), which packs the most-gathered entries of a pull together.
+    // perm[new] = old, iperm[old] = new.  Both halves are stored in the new
+    // labels; every entry keeps its position inside its block.
+    gtc::DevBuf<uint32_t> perm, iperm;
     gtc::Halves out;  // CSR: out-halves (out_edges order)
     gtc::Halves in;   // CSC: in-halves (in_edges order, the pull order)
-    gtc::Schedule sched_in, sched_out;
+    gtc::Units units_in, units_out;  // pull schedules of the plain and reversed views
     uint64_t launches = 0;  // kernels this handle has launched (diagnostics)
 };
 

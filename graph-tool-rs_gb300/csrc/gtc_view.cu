@@ -41,10 +41,12 @@ __global__ void k_remap_off(uint32_t n, const uint32_t* __restrict__ off,
     if (v <= n) foff[v] = pos[off[v]];
 }
 
-__global__ void k_active(uint32_t n, const uint8_t* __restrict__ vmask, uint8_t* __restrict__ act,
+// act[new] = vmask[perm[new]] != 0 (the caller's mask is by original index)
+__global__ void k_active(uint32_t n, const uint8_t* __restrict__ vmask,
+                         const uint32_t* __restrict__ perm, uint8_t* __restrict__ act,
                          uint32_t* __restrict__ count) {
     size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool a = v < n && vmask[v] != 0;
+    bool a = v < n && vmask[perm[v]] != 0;
     if (v < n) act[v] = a ? 1 : 0;
     unsigned b = __ballot_sync(0xffffffffu, a);
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned)__popc(b));
@@ -108,8 +110,8 @@ void View::prepare(gtc_graph* g, const gtc_view* v, cudaStream_t s, uint64_t* L)
         DevBuf<uint32_t> cnt(1, s);
         GTC_CUDA(cudaMemsetAsync(cnt.get(), 0, sizeof(uint32_t), s));
         if (n) {
-            k_active<<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, dv.get(), active.get(),
-                                                                cnt.get());
+            k_active<<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, dv.get(), g->perm.get(),
+                                                                active.get(), cnt.get());
             GTC_LAUNCHED();
             *L += 1;
         }
@@ -119,9 +121,10 @@ void View::prepare(gtc_graph* g, const gtc_view* v, cudaStream_t s, uint64_t* L)
         de.alloc(g->m, s);
         GTC_CUDA(cudaMemcpyAsync(de.get(), he, g->m, cudaMemcpyHostToDevice, s));
     }
-    compact_half(n, g->m, pull_src.off.get(), pull_src.other.get(), pull_src.eid.get(), dv.get(),
+    const uint8_t* vnew = hv ? active.get() : nullptr;  // the mask in internal labels
+    compact_half(n, g->m, pull_src.off.get(), pull_src.other.get(), pull_src.eid.get(), vnew,
                  de.get(), fpull, s, L);
-    compact_half(n, g->m, push_src.off.get(), push_src.other.get(), push_src.eid.get(), dv.get(),
+    compact_half(n, g->m, push_src.off.get(), push_src.other.get(), push_src.eid.get(), vnew,
                  de.get(), fpush, s, L);
     GTC_CUDA(cudaStreamSynchronize(s));
     pull_off = fpull.off.get(), pull_other = fpull.other.get(), pull_eid = fpull.eid.get();
