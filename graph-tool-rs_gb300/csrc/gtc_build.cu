@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(RS_NT) k_radix_scatter(
 
 // Stable sort of the index sequence 0..n-1 by keys[] (all keys < key_bound).
 // keys_out receives the sorted keys, vals_out the original positions.
-static void sort_positions_by_key(const uint32_t* keys, size_t n, uint32_t key_bound,
+void sort_positions_by_key(const uint32_t* keys, size_t n, uint32_t key_bound,
                                   uint32_t* keys_out, uint32_t* vals_out, cudaStream_t s,
                                   uint64_t* launches) {
     if (n == 0) return;

@@ -374,11 +374,11 @@ Units* pull_units(gtc_graph* g, const View& view, Units& local, cudaStream_t s) 
         Units& u = view.reversed ? g->units_out : g->units_in;
         if (!u.built) {
             GTC_CUDA(cudaStreamSynchronize(s));
-            build_units(view.pull_off, view.n, g->home, u);
+            build_units(view.pull_off, view.pull_other, view.pull_eid, view.n, g->home, u);
         }
         return &u;
     }
-    build_units(view.pull_off, view.n, s, local);
+    build_units(view.pull_off, view.pull_other, view.pull_eid, view.n, s, local);
     return &local;
 }
 
@@ -408,6 +408,10 @@ void launch_sweep(const SweepArgs& A, bool weighted, unsigned nb, cudaStream_t s
 void set_schedule(SweepArgs& A, const Units& u, const View& view) {
     A.units = u.units.get();
     A.longs = u.longs.get();
+    A.med = u.med.get();
+    A.slice_rows = u.slice_rows.get();
+    A.slice_off = u.slice_off.get();
+    A.sidx = u.sidx.get();
     A.partial = u.partial.get();
     A.counter = u.counter.get();
     A.long_out = u.long_out.get();
@@ -415,6 +419,28 @@ void set_schedule(SweepArgs& A, const Units& u, const View& view) {
     A.n_long = u.n_long;
     A.off = view.pull_off;
     A.other = view.pull_other;
+}
+
+// Weights of the sliced entries (0 for padding), per call.
+__global__ void k_gather_sw(uint32_t q, const uint32_t* __restrict__ seid, const void* __restrict__ w,
+                            int wdt, float* __restrict__ out) {
+    size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < q) {
+        const uint32_t e = seid[p];
+        out[p] = e != 0xFFFFFFFFu ? (float)ld_any(w, wdt, e) : 0.f;
+    }
+}
+
+DevBuf<float> sliced_weights(const Units& u, const SolveIn& in, cudaStream_t s, uint64_t* L) {
+    DevBuf<float> sw;
+    if (in.weight.present() && u.n_sliced) {
+        sw.alloc(u.n_sliced, s);
+        k_gather_sw<<<grid_for(u.n_sliced, 256, 1u << 30), 256, 0, s>>>(
+            u.n_sliced, u.seid.get(), in.weight.p, in.weight.dtype, sw.get());
+        GTC_LAUNCHED();
+        (*L)++;
+    }
+    return sw;
 }
 
 // Everything a sweep loop needs that does not change between sweeps.
@@ -581,7 +607,11 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
             GTC_LAUNCHED();
             L++;
         }
-        DevBuf<float> r0(n, s), r1(n, s), y0(n, s), y1(n, s);
+        // the gathered vectors carry one more entry, kept 0: the slices'
+        // padding gathers it
+        DevBuf<float> r0(n, s), r1(n, s), y0((size_t)n + 1, s), y1((size_t)n + 1, s);
+        GTC_CUDA(cudaMemsetAsync(y0.get() + n, 0, sizeof(float), s));
+        GTC_CUDA(cudaMemsetAsync(y1.get() + n, 0, sizeof(float), s));
         if (n) {
             k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.x64.get(), GTC_F64, nullptr,
                                                               r0.get());
@@ -607,6 +637,8 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         GTC_CUDA(cudaMemcpyAsync(dq + 1, dp + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
         SweepArgs A{};
         set_schedule(A, *U, view);
+        DevBuf<float> swt = sliced_weights(*U, in, s, &L);
+        A.sw = swt.get();
         A.w = wpull.get();
         A.active = act;
         A.invdeg = invdeg.get();
@@ -704,7 +736,9 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         store_result<double>(g, n, cur, P, in, s, &L);
     } else {
         DevBuf<float> wpull = pull_weights<float>(P, in, s, &L);
-        DevBuf<float> x0(n, s), x1(n, s);
+        DevBuf<float> x0((size_t)n + 1, s), x1((size_t)n + 1, s);  // x[n] == 0: slice padding
+        GTC_CUDA(cudaMemsetAsync(x0.get() + n, 0, sizeof(float), s));
+        GTC_CUDA(cudaMemsetAsync(x1.get() + n, 0, sizeof(float), s));
         if (n) {
             k_to_f32<<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, P.x64.get(), GTC_F64, nullptr,
                                                                 x0.get());
@@ -723,6 +757,8 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         float *xc = x0.get(), *xn = x1.get();
         SweepArgs A{};
         set_schedule(A, *U, view);
+        DevBuf<float> swt = sliced_weights(*U, in, s, &L);
+        A.sw = swt.get();
         A.w = wpull.get();
         A.active = act;
         A.part_a = f1.pa.get();

@@ -101,15 +101,21 @@ struct Halves {
     DevBuf<uint32_t> off, other, eid;
 };
 
-// Pull schedule of one half: its rows cut into work units of at most a
-// fixed number of merge items (rows + entries); see gtc_sweep.cuh.
+// Pull schedule of one half (gtc_sweep.cuh): rows split into sliced rows,
+// medium rows and long rows, and the work list over them.
 struct Units {
-    DevBuf<uint4> units;       // the work list
-    DevBuf<uint4> longs;       // per long row: {row, first chunk slot, chunks, 0}
-    DevBuf<float2> partial;    // per long chunk: compensated partial (s, c)
-    DevBuf<unsigned> counter;  // per long row: chunks done (reset by the last)
-    DevBuf<double2> long_out;  // per long row: its epilogue's reduction terms
-    uint32_t n_units = 0, n_long = 0, n_chunks = 0;
+    DevBuf<uint4> units;         // the work list
+    DevBuf<uint4> longs;         // per long row: {row, first chunk slot, chunks, 0}
+    DevBuf<float2> partial;      // per long chunk: compensated partial (s, c)
+    DevBuf<unsigned> counter;    // per long row: chunks done (reset by the last)
+    DevBuf<double2> long_out;    // per long row: its epilogue's reduction terms
+    DevBuf<uint32_t> med;        // medium rows
+    DevBuf<uint32_t> slice_rows; // 32 rows per slice (NO_ROW pads)
+    DevBuf<uint32_t> slice_off;  // first sliced entry of each slice, n_slices + 1
+    DevBuf<uint32_t> sidx;       // sliced entries: source vertex (n pads)
+    DevBuf<uint32_t> seid;       // sliced entries: edge id (0xFFFFFFFF pads)
+    uint32_t n_units = 0, n_long = 0, n_chunks = 0, n_med = 0, n_slices = 0;
+    uint32_t n_sliced = 0;       // sliced entries including padding
     bool built = false;
 };
 
@@ -169,6 +175,12 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
               cudaStream_t s);
 void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* res,
                  cudaStream_t s);
+
+// Stable sort of the positions 0..n-1 by keys[] (every key < key_bound):
+// keys_out gets the sorted keys, vals_out the positions (gtc_build.cu).
+void sort_positions_by_key(const uint32_t* keys, size_t n, uint32_t key_bound,
+                           uint32_t* keys_out, uint32_t* vals_out, cudaStream_t s,
+                           uint64_t* launches);
 
 // scans (gtc_build.cu): exclusive scan of n u32 values into out[0..n],
 // out[n] = total.  `out` may alias `in` only if the caller passes the same
