@@ -19,6 +19,7 @@
 // an add.  Results are bit-identical to the reference's for the same Plan.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "gtc_sweep.cuh"
 #include "gtc_view.cuh"
@@ -382,27 +383,99 @@ Units* pull_units(gtc_graph* g, const View& view, Units& local, cudaStream_t s) 
     return &local;
 }
 
-template <int MODE, bool W>
-unsigned sweep_grid(uint32_t n_units) {
+// Entries staged in shared memory by the HOT variant: the whole vector when
+// it fits, else the hottest prefix; a multiple of 4 (float4 staging).
+inline uint32_t hot_entries(uint32_t n) {
+    const uint32_t h = n < (uint32_t)SP_HOT ? n : (uint32_t)SP_HOT;
+    return h & ~3u;
+}
+
+// The kernel variants the autotuner chooses between.
+enum SweepVariant { VAR_L1 = 0, VAR_HOT = 1, N_VARIANTS = 2 };
+
+struct VariantShape {
+    unsigned grid, threads;
+    size_t smem;
+};
+
+template <int MODE, bool W, int NT, bool HOT>
+VariantShape variant_shape(uint32_t n_units, uint32_t hot_n) {
     static int per_sm = 0, sms = 0;
+    const int dyn_max = HOT ? SP_HOT * (int)sizeof(float) : 0;
     if (!per_sm) {
         int dev = 0;
         GTC_CUDA(cudaGetDevice(&dev));
         GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<MODE, W>, SP_NT, 0));
+        if (HOT)
+            GTC_CUDA(cudaFuncSetAttribute(k_sweep<MODE, W, NT, HOT>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_max));
+        GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<MODE, W, NT, HOT>,
+                                                               NT, dyn_max));
         if (per_sm < 1) per_sm = 1;
     }
     const unsigned cap = (unsigned)(per_sm * sms);
-    return n_units < 1 ? 1u : (n_units < cap ? n_units : cap);
+    const unsigned want = (n_units + NT / 32 - 1) / (NT / 32);
+    VariantShape v;
+    v.grid = want < 1 ? 1u : (want < cap ? want : cap);
+    v.threads = NT;
+    v.smem = HOT ? (size_t)hot_n * sizeof(float) : 0;
+    return v;
+}
+
+template <int MODE, bool W>
+void launch_variant(int var, const SweepArgs& A, cudaStream_t s) {
+    if (var == VAR_HOT) {
+        VariantShape v = variant_shape<MODE, W, 1024, true>(A.n_units, A.hot_n);
+        k_sweep<MODE, W, 1024, true><<<v.grid, v.threads, v.smem, s>>>(A);
+    } else {
+        VariantShape v = variant_shape<MODE, W, 256, false>(A.n_units, A.hot_n);
+        k_sweep<MODE, W, 256, false><<<v.grid, v.threads, v.smem, s>>>(A);
+    }
+    GTC_LAUNCHED();
 }
 
 template <int MODE>
-void launch_sweep(const SweepArgs& A, bool weighted, unsigned nb, cudaStream_t s) {
+void launch_sweep(int var, const SweepArgs& A, bool weighted, cudaStream_t s) {
     if (weighted)
-        k_sweep<MODE, true><<<nb, SP_NT, 0, s>>>(A);
+        launch_variant<MODE, true>(var, A, s);
     else
-        k_sweep<MODE, false><<<nb, SP_NT, 0, s>>>(A);
-    GTC_LAUNCHED();
+        launch_variant<MODE, false>(var, A, s);
+}
+
+// The autotuner: the first sweep of a (graph half, mode, weighting) runs every
+// variant once on the real inputs (a sweep only reads prev and writes next,
+// so the trial is harmless), keeps the fastest and caches the choice on the
+// graph.  The variants compute bit-identical results (same per-item order and
+// fold), so the choice changes speed only.
+template <int MODE>
+int tuned_variant(Units& u, const SweepArgs& A, bool weighted, cudaStream_t s, uint64_t* L) {
+    int& v = u.variant[MODE][weighted ? 1 : 0];
+    if (v >= 0) return v;
+    if (const char* e = std::getenv("GTC_SWEEP_VARIANT")) {  // pinned for experiments
+        v = std::atoi(e) == 1 ? VAR_HOT : VAR_L1;
+        return v;
+    }
+    cudaEvent_t e0, e1;
+    GTC_CUDA(cudaEventCreate(&e0));
+    GTC_CUDA(cudaEventCreate(&e1));
+    float best = 0.f;
+    int best_v = VAR_L1;
+    for (int rep = 0; rep < 2; ++rep) {  // the first round warms caches up
+        for (int c = 0; c < N_VARIANTS; ++c) {
+            GTC_CUDA(cudaEventRecord(e0, s));
+            launch_sweep<MODE>(c, A, weighted, s);
+            GTC_CUDA(cudaEventRecord(e1, s));
+            GTC_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            GTC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            *L += 1;
+            if (rep == 1 && (c == 0 || ms < best)) best = ms, best_v = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    v = best_v;
+    return v;
 }
 
 void set_schedule(SweepArgs& A, const Units& u, const View& view) {
@@ -415,10 +488,12 @@ void set_schedule(SweepArgs& A, const Units& u, const View& view) {
     A.partial = u.partial.get();
     A.counter = u.counter.get();
     A.long_out = u.long_out.get();
+    A.item_out = u.item_out.get();
     A.n_units = u.n_units;
     A.n_long = u.n_long;
     A.off = view.pull_off;
     A.other = view.pull_other;
+    A.hot_n = hot_entries(view.n);
 }
 
 // Weights of the sliced entries (0 for padding), per call.
@@ -627,11 +702,9 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         L++;
         float *rc = r0.get(), *rn = r1.get(), *yc = y0.get(), *yn = y1.get();
         Units local;
-        const Units* U = pull_units(g, view, local, s);
+        Units* U = pull_units(g, view, local, s);
         const bool W = in.weight.present();
-        const unsigned grid = W ? sweep_grid<MODE_PAGERANK, true>(U->n_units)
-                                : sweep_grid<MODE_PAGERANK, false>(U->n_units);
-        FoldBufs fs(grid, s);
+        FoldBufs fs(1, s);
         double* dq = fs.out.get();
         // the dangling mass of the initial iterate seeds the first sweep
         GTC_CUDA(cudaMemcpyAsync(dq + 1, dp + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -648,15 +721,17 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         A.one_minus_d = (float)(1.0 - d);
         A.d = (float)d;
         A.psink = dq + 1;
-        A.part_a = fs.pa.get();
-        A.part_b = fs.pb.get();
         A.ticket = fs.ticket.get();
         A.out = dq;
+        A.x = yc, A.prev = rc, A.next = rn, A.ynext = yn;
+        const int var = tuned_variant<MODE_PAGERANK>(*U, A, W, s, &L);
+        // a tuning trial wrote the dangling mass of its output: restore it
+        GTC_CUDA(cudaMemcpyAsync(dq + 1, dp + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
         total.start();
         while (delta >= eps) {
             A.x = yc, A.prev = rc, A.next = rn, A.ynext = yn;
             if (in.timing) sw.start();
-            launch_sweep<MODE_PAGERANK>(A, W, grid, s);
+            launch_sweep<MODE_PAGERANK>(var, A, W, s);
             if (in.timing) sw.stop();
             L++;
             SL++;
@@ -746,12 +821,10 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
             L++;
         }
         Units local;
-        const Units* U = pull_units(g, view, local, s);
+        Units* U = pull_units(g, view, local, s);
         const bool W = in.weight.present();
-        const unsigned grid = W ? sweep_grid<MODE_EIGEN, true>(U->n_units)
-                                : sweep_grid<MODE_EIGEN, false>(U->n_units);
         const unsigned nb = persistent_blocks(n);
-        FoldBufs f1(grid, s), f2(nb, s);
+        FoldBufs f1(1, s), f2(nb, s);
         double* o1 = f1.out.get();
         double* o2 = f2.out.get();
         float *xc = x0.get(), *xn = x1.get();
@@ -761,15 +834,15 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         A.sw = swt.get();
         A.w = wpull.get();
         A.active = act;
-        A.part_a = f1.pa.get();
-        A.part_b = f1.pb.get();
         A.ticket = f1.ticket.get();
         A.out = o1;
+        A.x = xc, A.prev = xc, A.next = xn;
+        const int var = tuned_variant<MODE_EIGEN>(*U, A, W, s, &L);
         total.start();
         while (delta >= eps) {
             A.x = xc, A.prev = xc, A.next = xn;
             if (in.timing) sw.start();
-            launch_sweep<MODE_EIGEN>(A, W, grid, s);
+            launch_sweep<MODE_EIGEN>(var, A, W, s);
             k_ev_f32_norm<<<nb, PR_NT, 0, s>>>(n, act, o1, xc, xn, f2.fold(o2, o2 + 1));
             GTC_LAUNCHED();
             if (in.timing) sw.stop();

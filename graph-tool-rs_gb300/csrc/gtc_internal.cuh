@@ -109,6 +109,7 @@ struct Units {
     DevBuf<float2> partial;      // per long chunk: compensated partial (s, c)
     DevBuf<unsigned> counter;    // per long row: chunks done (reset by the last)
     DevBuf<double2> long_out;    // per long row: its epilogue's reduction terms
+    DevBuf<double2> item_out;    // per work item: its rows' reduction terms
     DevBuf<uint32_t> med;        // medium rows
     DevBuf<uint32_t> slice_rows; // 32 rows per slice (NO_ROW pads)
     DevBuf<uint32_t> slice_off;  // first sliced entry of each slice, n_slices + 1
@@ -116,6 +117,7 @@ struct Units {
     DevBuf<uint32_t> seid;       // sliced entries: edge id (0xFFFFFFFF pads)
     uint32_t n_units = 0, n_long = 0, n_chunks = 0, n_med = 0, n_slices = 0;
     uint32_t n_sliced = 0;       // sliced entries including padding
+    int variant[2][2] = {{-1, -1}, {-1, -1}};  // tuned kernel variant [mode][weighted]
     bool built = false;
 };
 

@@ -175,7 +175,8 @@ void build_units(const uint32_t* d_off, const uint32_t* d_other, const uint32_t*
         GTC_CUDA(cudaStreamSynchronize(s));
     }
 
-    // ---- the work list: long chunks, then medium rows, then slices ----
+    // ---- the work list (one warp per item): long chunks, then medium rows,
+    // then slices, so the heaviest items are spread over the warps first ----
     std::vector<uint4> units, longs;
     uint32_t slot = 0;
     for (uint32_t k = 0; k < nl; ++k) {
@@ -185,10 +186,8 @@ void build_units(const uint32_t* d_off, const uint32_t* d_other, const uint32_t*
         for (uint32_t c = 0; c < chunks; ++c) units.push_back(make_uint4(UNIT_LONG, k, c, 0));
         slot += chunks;
     }
-    for (uint32_t q = 0; q < u.n_med; q += SP_WARPS)
-        units.push_back(make_uint4(UNIT_MEDIUM, q, std::min(q + SP_WARPS, u.n_med), 0));
-    for (uint32_t k = 0; k < n_slices; k += SLICES_PER_UNIT)
-        units.push_back(make_uint4(UNIT_SLICES, k, std::min(k + SLICES_PER_UNIT, n_slices), 0));
+    for (uint32_t q = 0; q < u.n_med; ++q) units.push_back(make_uint4(UNIT_MEDIUM, q, 0, 0));
+    for (uint32_t k = 0; k < n_slices; ++k) units.push_back(make_uint4(UNIT_SLICES, k, 0, 0));
 
     u.n_units = (uint32_t)units.size();
     u.n_long = (uint32_t)longs.size();
@@ -198,6 +197,8 @@ void build_units(const uint32_t* d_off, const uint32_t* d_other, const uint32_t*
     u.partial.alloc(slot, s);
     u.counter.alloc(longs.size(), s);
     u.long_out.alloc(longs.size(), s);
+    const size_t n_buckets = (units.size() + SP_BUCKET - 1) / SP_BUCKET;
+    u.item_out.alloc(n_buckets, s);
     if (!units.empty())
         GTC_CUDA(cudaMemcpyAsync(u.units.get(), units.data(), units.size() * sizeof(uint4),
                                  cudaMemcpyHostToDevice, s));

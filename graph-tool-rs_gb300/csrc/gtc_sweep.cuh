@@ -27,18 +27,22 @@
 
 namespace gtc {
 
-constexpr int SP_NT = 256;
-constexpr int SP_WARPS = SP_NT / 32;
 constexpr int SP_CAP = 2048;        // entries per long-row chunk; longest medium row
+// Variant with a shared-memory copy of the hottest entries of the gathered
+// vector: vertices are labelled by descending out-degree, so its first
+// SP_HOT entries are the most gathered ones (the rest is read through
+// L1/L2).  One 1024-thread CTA per SM holds them.
+constexpr int SP_HOT = 32768;
+constexpr int SP_FOLD = 256;        // fixed fan-in of the final reduction
+constexpr int SP_BUCKET = 8;        // work items a warp takes together (one fold term)
 constexpr int SP_SLICE_MAX = 128;   // longest row kept in a slice
 constexpr int SP_WINDOW = 2048;     // rows sorted by length inside windows of this many
 constexpr uint32_t NO_ROW = 0xFFFFFFFFu;
 
-// Work-unit kinds (uint4.x); .y/.z as described.
+// Work items, one warp each (uint4.x = kind; .y/.z as described).
 constexpr uint32_t UNIT_LONG = 1;    // long row index y, chunk z
-constexpr uint32_t UNIT_MEDIUM = 2;  // medium rows med[y .. z), one per warp
-constexpr uint32_t UNIT_SLICES = 3;  // slices [y, z), strided over the warps
-constexpr uint32_t SLICES_PER_UNIT = 4 * SP_WARPS;
+constexpr uint32_t UNIT_MEDIUM = 2;  // medium row med[y]
+constexpr uint32_t UNIT_SLICES = 3;  // slice y
 
 // Cut the rows of a pull half into the three tiers and the work list.
 void build_units(const uint32_t* d_off, const uint32_t* d_other, const uint32_t* d_eid,
@@ -59,6 +63,8 @@ struct SweepArgs {
     unsigned* counter;
     double2* long_out;
     uint32_t n_units, n_long;
+    uint32_t hot_n;     // entries of x staged in shared memory (HOT variant)
+    double2* item_out;  // per bucket of SP_BUCKET items: its rows' reduction terms
     // pull half (medium and long rows)
     const uint32_t* __restrict__ off;
     const uint32_t* __restrict__ other;
@@ -74,9 +80,7 @@ struct SweepArgs {
     const float* __restrict__ pers;     // PageRank only (null = uniform)
     float uniform, one_minus_d, d;
     const double* psink;                // PageRank: dangling mass of prev
-    // reduction: per-CTA partials, folded by the last CTA
-    double* part_a;
-    double* part_b;
+    // reduction: every item's terms, folded by the last CTA
     unsigned* ticket;
     double* out;  // [a, b]
 };
@@ -128,184 +132,217 @@ __device__ __forceinline__ void sweep_row(const SweepArgs& A, uint32_t v, float 
     }
 }
 
-template <int MODE, bool WEIGHTED>
-__global__ void __launch_bounds__(SP_NT, 6) k_sweep(SweepArgs A) {
-    __shared__ float2 red[SP_WARPS];
-    __shared__ double fa[SP_WARPS], fb[SP_WARPS];
+template <bool HOT>
+__device__ __forceinline__ float gather(const SweepArgs& A, const float* hot, uint32_t s) {
+    return (HOT && s < A.hot_n) ? hot[s] : __ldg(A.x + s);
+}
+
+// Warp sum of a (ta, tb) pair in a fixed shuffle order, as TwoSum pairs.
+__device__ __forceinline__ double2 warp_pair(float ta, float tb) {
+    Kahan ka, kb;
+    ka.s = ta, kb.s = tb;
+    warp_merge_kahan(ka);
+    warp_merge_kahan(kb);
+    return make_double2((double)ka.s + (double)ka.c, (double)kb.s + (double)kb.c);
+}
+
+// NT threads per CTA; HOT: stage x[0 .. hot_n) in shared memory.
+template <int MODE, bool WEIGHTED, int NT, bool HOT>
+__global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
+    constexpr int SP_WARPS = NT / 32;
+    extern __shared__ float hot[];  // x[0 .. hot_n)
+    __shared__ double fa[SP_FOLD], fb[SP_FOLD];
     __shared__ bool flag;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float psink = MODE == MODE_PAGERANK ? (float)*A.psink : 0.f;
-    KahanLite acc_a, acc_b;
+    if (HOT) {
+        const float4* src = reinterpret_cast<const float4*>(A.x);
+        float4* dst = reinterpret_cast<float4*>(hot);
+        const uint32_t n4 = A.hot_n / 4;  // hot_n is a multiple of 4
+        for (uint32_t i = tid; i < n4; i += NT) dst[i] = __ldg(src + i);
+        __syncthreads();
+    }
+    const bool H = HOT && A.hot_n != 0;
 
-    for (uint32_t u = blockIdx.x; u < A.n_units; u += gridDim.x) {
+    const uint32_t gw = blockIdx.x * SP_WARPS + warp, nw = gridDim.x * SP_WARPS;
+    // A warp takes buckets of up to SP_BUCKET items, bucket b being items
+    // b, b + B, b + 2B, ... (B buckets): every bucket mixes heavy and light
+    // items.  The terms of a bucket's rows go to item_out[b] (long rows:
+    // long_out[k]) and the last CTA folds them with a fixed fan-in, so neither
+    // the grid nor the CTA size changes a single bit of the result.
+    const uint32_t n_buckets = (A.n_units + SP_BUCKET - 1) / SP_BUCKET;
+    for (uint32_t bk = gw; bk < n_buckets; bk += nw) {
+    KahanLite bucket_a, bucket_b;
+    for (uint32_t u = bk; u < A.n_units; u += n_buckets) {
         const uint4 U = A.units[u];
         if (U.x == UNIT_SLICES) {
-            // this warp's slices: U.y + warp, + SP_WARPS, ...
-            for (uint32_t k = U.y + warp; k < U.z; k += SP_WARPS) {
-                const uint32_t b = __ldg(A.slice_off + k);
-                const uint32_t len = (__ldg(A.slice_off + k + 1) - b) >> 5;
-                const uint32_t row = __ldg(A.slice_rows + 32 * k + lane);
-                const uint32_t* ip = A.sidx + b + lane;
-                const float* wp = WEIGHTED ? A.sw + b + lane : nullptr;
-                KahanLite acc;
-                uint32_t j = 0;
-                for (; j + 4 <= len; j += 4) {
-                    const uint32_t s0 = __ldcs(ip), s1 = __ldcs(ip + 32), s2 = __ldcs(ip + 64),
-                                   s3 = __ldcs(ip + 96);
-                    float v0 = A.x[s0], v1 = A.x[s1], v2 = A.x[s2], v3 = A.x[s3];
-                    if (WEIGHTED) {
-                        v0 = __fmul_rn(v0, __ldcs(wp));
-                        v1 = __fmul_rn(v1, __ldcs(wp + 32));
-                        v2 = __fmul_rn(v2, __ldcs(wp + 64));
-                        v3 = __fmul_rn(v3, __ldcs(wp + 96));
-                        wp += 128;
-                    }
-                    acc.add(v0);
-                    acc.add(v1);
-                    acc.add(v2);
-                    acc.add(v3);
-                    ip += 128;
+            const uint32_t k = U.y;
+            const uint32_t b = __ldg(A.slice_off + k);
+            const uint32_t len = (__ldg(A.slice_off + k + 1) - b) >> 5;
+            const uint32_t row = __ldg(A.slice_rows + 32 * k + lane);
+            const uint32_t* ip = A.sidx + b + lane;
+            const float* wp = WEIGHTED ? A.sw + b + lane : nullptr;
+            KahanLite acc;
+            uint32_t j = 0;
+            for (; j + 4 <= len; j += 4) {
+                const uint32_t s0 = __ldcs(ip), s1 = __ldcs(ip + 32), s2 = __ldcs(ip + 64),
+                               s3 = __ldcs(ip + 96);
+                float v0, v1, v2, v3;
+                if (H) {
+                    v0 = gather<HOT>(A, hot, s0), v1 = gather<HOT>(A, hot, s1);
+                    v2 = gather<HOT>(A, hot, s2), v3 = gather<HOT>(A, hot, s3);
+                } else {
+                    v0 = __ldg(A.x + s0), v1 = __ldg(A.x + s1);
+                    v2 = __ldg(A.x + s2), v3 = __ldg(A.x + s3);
                 }
-                for (; j < len; ++j) {
-                    float v = A.x[__ldcs(ip)];
-                    if (WEIGHTED) {
-                        v = __fmul_rn(v, __ldcs(wp));
-                        wp += 32;
-                    }
-                    acc.add(v);
-                    ip += 32;
+                if (WEIGHTED) {
+                    v0 = __fmul_rn(v0, __ldcs(wp));
+                    v1 = __fmul_rn(v1, __ldcs(wp + 32));
+                    v2 = __fmul_rn(v2, __ldcs(wp + 64));
+                    v3 = __fmul_rn(v3, __ldcs(wp + 96));
+                    wp += 128;
                 }
-                if (row != NO_ROW) {
-                    float ta, tb;
-                    sweep_row<MODE>(A, row, acc.value(), psink, ta, tb);
-                    acc_a.add(ta);
-                    acc_b.add(tb);
-                }
+                acc.add(v0);
+                acc.add(v1);
+                acc.add(v2);
+                acc.add(v3);
+                ip += 128;
             }
-        } else if (U.x == UNIT_MEDIUM) {
-            const uint32_t q = U.y + warp;
-            if (q < U.z) {
-                const uint32_t row = __ldg(A.med + q);
-                const uint32_t b = __ldg(A.off + row), e = __ldg(A.off + row + 1);
-                KahanLite kl;
-                uint32_t p = b + lane;
-                for (; p + 96 < e; p += 128) {
-                    const uint32_t s0 = __ldcs(A.other + p), s1 = __ldcs(A.other + p + 32),
-                                   s2 = __ldcs(A.other + p + 64), s3 = __ldcs(A.other + p + 96);
-                    float v0 = A.x[s0], v1 = A.x[s1], v2 = A.x[s2], v3 = A.x[s3];
-                    if (WEIGHTED) {
-                        v0 = __fmul_rn(v0, __ldcs(A.w + p));
-                        v1 = __fmul_rn(v1, __ldcs(A.w + p + 32));
-                        v2 = __fmul_rn(v2, __ldcs(A.w + p + 64));
-                        v3 = __fmul_rn(v3, __ldcs(A.w + p + 96));
-                    }
-                    kl.add(v0);
-                    kl.add(v1);
-                    kl.add(v2);
-                    kl.add(v3);
+            for (; j < len; ++j) {
+                float v = gather<HOT>(A, hot, __ldcs(ip));
+                if (WEIGHTED) {
+                    v = __fmul_rn(v, __ldcs(wp));
+                    wp += 32;
                 }
-                for (; p < e; p += 32) {
-                    float v = A.x[__ldcs(A.other + p)];
-                    if (WEIGHTED) v = __fmul_rn(v, __ldcs(A.w + p));
-                    kl.add(v);
-                }
-                Kahan k = kl.full();
-                warp_merge_kahan(k);
-                if (lane == 0) {
-                    float ta, tb;
-                    sweep_row<MODE>(A, row, k.value(), psink, ta, tb);
-                    acc_a.add(ta);
-                    acc_b.add(tb);
-                }
+                acc.add(v);
+                ip += 32;
             }
-        } else {  // UNIT_LONG
-            const uint4 LR = A.longs[U.y];
-            const uint32_t row = LR.x, c = U.z;
-            const uint32_t b = __ldg(A.off + row) + c * SP_CAP;
-            const uint32_t e = min(b + (uint32_t)SP_CAP, __ldg(A.off + row + 1));
-            constexpr int IPT = SP_CAP / SP_NT;
-            uint32_t idx[IPT];
-            float wv[IPT];
-#pragma unroll
-            for (int k = 0; k < IPT; ++k) {
-                const uint32_t p = b + tid + k * SP_NT;
-                idx[k] = p < e ? __ldcs(A.other + p) : 0u;
-                if (WEIGHTED) wv[k] = p < e ? __ldcs(A.w + p) : 0.f;
+            if (row != NO_ROW) {
+                float ta, tb;
+                sweep_row<MODE>(A, row, acc.value(), psink, ta, tb);
+                bucket_a.add(ta);
+                bucket_b.add(tb);
+            }
+        } else {
+            // a medium row, or one chunk of a long row: lanes stride entries
+            uint32_t row, b, e;
+            uint4 LR = make_uint4(0, 0, 0, 0);
+            if (U.x == UNIT_MEDIUM) {
+                row = __ldg(A.med + U.y);
+                b = __ldg(A.off + row), e = __ldg(A.off + row + 1);
+            } else {
+                LR = A.longs[U.y];
+                row = LR.x;
+                b = __ldg(A.off + row) + U.z * SP_CAP;
+                e = min(b + (uint32_t)SP_CAP, __ldg(A.off + row + 1));
             }
             KahanLite kl;
-#pragma unroll
-            for (int k = 0; k < IPT; ++k) {
-                const uint32_t p = b + tid + k * SP_NT;
-                if (p < e) {
-                    const float xv = A.x[idx[k]];
-                    kl.add(WEIGHTED ? __fmul_rn(xv, wv[k]) : xv);
+            uint32_t p = b + lane;
+            for (; p + 96 < e; p += 128) {
+                const uint32_t s0 = __ldcs(A.other + p), s1 = __ldcs(A.other + p + 32),
+                               s2 = __ldcs(A.other + p + 64), s3 = __ldcs(A.other + p + 96);
+                float v0 = gather<HOT>(A, hot, s0), v1 = gather<HOT>(A, hot, s1);
+                float v2 = gather<HOT>(A, hot, s2), v3 = gather<HOT>(A, hot, s3);
+                if (WEIGHTED) {
+                    v0 = __fmul_rn(v0, __ldcs(A.w + p));
+                    v1 = __fmul_rn(v1, __ldcs(A.w + p + 32));
+                    v2 = __fmul_rn(v2, __ldcs(A.w + p + 64));
+                    v3 = __fmul_rn(v3, __ldcs(A.w + p + 96));
                 }
+                kl.add(v0);
+                kl.add(v1);
+                kl.add(v2);
+                kl.add(v3);
+            }
+            for (; p < e; p += 32) {
+                float v = gather<HOT>(A, hot, __ldcs(A.other + p));
+                if (WEIGHTED) v = __fmul_rn(v, __ldcs(A.w + p));
+                kl.add(v);
             }
             Kahan k = kl.full();
             warp_merge_kahan(k);
-            if (lane == 0) red[warp] = make_float2(k.s, k.c);
-            __syncthreads();
-            if (tid == 0) {
-                Kahan t;
-                for (int w = 0; w < SP_WARPS; ++w) t.merge(red[w].x, red[w].y);
-                A.partial[LR.y + c] = make_float2(t.s, t.c);
-                __threadfence();
-                const unsigned done = atomicAdd(&A.counter[U.y], 1u);
-                flag = (done == LR.z - 1);
-            }
-            __syncthreads();
-            if (flag && tid == 0) {
-                __threadfence();
-                Kahan t;
-                for (uint32_t q = 0; q < LR.z; ++q) {
-                    const float2 pq = __ldcg(&A.partial[LR.y + q]);
-                    t.merge(pq.x, pq.y);
+            if (U.x == UNIT_MEDIUM) {
+                if (lane == 0) {
+                    float ta, tb;
+                    sweep_row<MODE>(A, row, k.value(), psink, ta, tb);
+                    bucket_a.add(ta);
+                    bucket_b.add(tb);
                 }
-                A.counter[U.y] = 0u;
-                float ta, tb;
-                sweep_row<MODE>(A, row, t.value(), psink, ta, tb);
-                // a long row's terms are folded by index, not by whichever
-                // CTA happened to finish it, so the sums stay deterministic
-                A.long_out[U.y] = make_double2((double)ta, (double)tb);
+            } else {
+                // long row: the last warp to finish a chunk folds the chunks
+                bool last = false;
+                if (lane == 0) {
+                    A.partial[LR.y + U.z] = make_float2(k.s, k.c);
+                    __threadfence();
+                    const unsigned done = atomicAdd(&A.counter[U.y], 1u);
+                    last = (done == LR.z - 1);
+                    if (last) {
+                        __threadfence();
+                        Kahan t;
+                        for (uint32_t q = 0; q < LR.z; ++q) {
+                            const float2 pq = __ldcg(&A.partial[LR.y + q]);
+                            t.merge(pq.x, pq.y);
+                        }
+                        A.counter[U.y] = 0u;
+                        float ta, tb;
+                        sweep_row<MODE>(A, row, t.value(), psink, ta, tb);
+                        // folded by row index, not by whichever warp finished
+                        A.long_out[U.y] = make_double2((double)ta, (double)tb);
+                    }
+                }
             }
-            __syncthreads();
         }
     }
 
-    // ---- deterministic fold: CTA partials, then long-row terms, in order ----
-    double a = (double)acc_a.s - (double)acc_a.c;
-    double b = (double)acc_b.s - (double)acc_b.c;
-    a = warp_sum_f64(a);
-    b = warp_sum_f64(b);
-    if (lane == 0) fa[warp] = a, fb[warp] = b;
+        const double2 it = warp_pair(bucket_a.value(), bucket_b.value());
+        if (lane == 0) A.item_out[bk] = it;
+    }
+
+    // ---- the last CTA folds every bucket's terms, then the long rows' ----
     __syncthreads();
     if (tid == 0) {
-        double ta = 0.0, tb = 0.0;
-        for (int w = 0; w < SP_WARPS; ++w) ta += fa[w], tb += fb[w];
-        A.part_a[blockIdx.x] = ta;
-        A.part_b[blockIdx.x] = tb;
         __threadfence();
         const unsigned t = atomicAdd(A.ticket, 1u);
         flag = (t == gridDim.x - 1);
     }
     __syncthreads();
-    if (flag && warp == 0) {
+    if (flag) {
         __threadfence();
-        double ta = 0.0, tb = 0.0;
-        for (unsigned i = lane; i < gridDim.x; i += 32) {
-            ta += __ldcg(A.part_a + i);
-            tb += __ldcg(A.part_b + i);
+        if (tid < SP_FOLD) {
+            // thread t folds a contiguous range, eight loads in flight
+            double ta = 0.0, tb = 0.0;
+            auto fold_range = [&](const double2* v, uint32_t cnt) {
+                const uint32_t per = (cnt + SP_FOLD - 1) / SP_FOLD;
+                const uint32_t b = min(tid * per, cnt), e = min(b + per, cnt);
+                uint32_t i = b;
+                for (; i + 8 <= e; i += 8) {
+                    double2 q[8];
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) q[t] = __ldcg(v + i + t);
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) ta += q[t].x, tb += q[t].y;
+                }
+                for (; i < e; ++i) {
+                    const double2 q = __ldcg(v + i);
+                    ta += q.x, tb += q.y;
+                }
+            };
+            fold_range(A.item_out, n_buckets);
+            fold_range(A.long_out, A.n_long);
+            fa[tid] = ta;
+            fb[tid] = tb;
         }
-        for (unsigned i = lane; i < A.n_long; i += 32) {
-            const double2 q = __ldcg(A.long_out + i);
-            ta += q.x;
-            tb += q.y;
+        __syncthreads();
+        for (int w = SP_FOLD / 2; w > 0; w >>= 1) {
+            if (tid < w) {
+                fa[tid] += fa[tid + w];
+                fb[tid] += fb[tid + w];
+            }
+            __syncthreads();
         }
-        ta = warp_sum_f64(ta);
-        tb = warp_sum_f64(tb);
-        if (lane == 0) {
-            A.out[0] = ta;
-            A.out[1] = tb;
+        if (tid == 0) {
+            A.out[0] = fa[0];
+            A.out[1] = fb[0];
             *A.ticket = 0u;
         }
     }
