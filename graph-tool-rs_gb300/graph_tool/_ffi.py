@@ -97,6 +97,9 @@ SIGNATURES = {
     "gtc_eigenvector_device": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(DVec),
                                          C.POINTER(PowerIteration), C.POINTER(DVec), C.c_uint64,
                                          C.POINTER(Options), C.POINTER(Result)]),
+    "gtc_pagerank_noalloc": (C.c_int, [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_double, C.c_double, C.c_uint64, C.c_void_p,
+                                       C.POINTER(C.c_uint64), C.c_void_p]),
 }
 
 _lib = None

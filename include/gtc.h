@@ -205,6 +205,36 @@ int gtc_eigenvector_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* w
                            const gtc_power_iteration* params, gtc_dvec* x, uint64_t x_had,
                            const gtc_options* opt, gtc_result* result);
 
+/* ---- PageRank without any allocation ------------------------------------
+ *
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory when they run PageRank (a runtime that reserved all
+ * GPU memory up front and forbids later allocations, or a code path where an
+ * allocation would stall or fail).  It calls no cudaMalloc, cudaFree or any
+ * other allocating routine: the caller passes the graph and the output, and
+ * every intermediate vector lives in one static device array compiled into
+ * the library (about 12.6 MB, held by every GPU that loads the library until
+ * the process exits).
+ *
+ *   n             vertices, at most 1,048,576 (larger n is GTC_ERR_ARG)
+ *   d_off, d_src  the pull adjacency in device memory: the in-edges of v are
+ *                 d_src[d_off[v] .. d_off[v+1]) (sources < n), the order the
+ *                 reference's in_edges yields (gtc_graph_export's in-halves)
+ *   d_out_degree  out-degree of every vertex (device, n entries)
+ *   d_rank        output, device, n floats: PageRank from the uniform start
+ *                 (pagerank with a Unity weight, centrality.rs:234-248)
+ *   stream        a cudaStream_t (NULL = the legacy default stream)
+ *
+ * FP32 vectors, compensated row sums, FP64 delta and dangling mass.  All
+ * calls share the static array and it keeps the last call's contents (each
+ * call clears what must start at zero); calls that overlap on the GPU race.
+ * The first call on a device looks the array's device address up, so make it
+ * before anything that must not see that call's synchronisation.  Returns
+ * when the result is in d_rank. */
+int gtc_pagerank_noalloc(uint64_t n, const uint32_t* d_off, const uint32_t* d_src,
+                         const uint32_t* d_out_degree, double damping, double epsilon,
+                         uint64_t max_iter, float* d_rank, uint64_t* iters_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
