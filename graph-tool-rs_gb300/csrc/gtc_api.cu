@@ -348,4 +348,90 @@ int gtc_eigenvector_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* w
     });
 }
 
+int gtc_pagerank_adjoint_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* weight,
+                                const gtc_dvec* pers, double damping,
+                                const gtc_power_iteration* params, const gtc_dvec* pi,
+                                const gtc_dvec* grad_pi, gtc_dvec* grad_weight, gtc_dvec* grad_pers,
+                                const gtc_options* opt, gtc_result* result) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        AdjointIn in{};
+        check_params(g, params, in.params);
+        in.weight = dvec_in(weight, g->m, "weight");
+        in.pers = dvec_in(pers, g->n, "personalisation");
+        GTC_REQUIRE(pi && (pi->ptr || g->n == 0), GTC_ERR_ARG, "pi is NULL");
+        GTC_REQUIRE(grad_pi && (grad_pi->ptr || g->n == 0), GTC_ERR_ARG, "grad_pi is NULL");
+        in.pi = dvec_in(pi, g->n, "pi");
+        in.gpi = dvec_in(grad_pi, g->n, "grad_pi");
+        if (grad_weight && grad_weight->ptr) {
+            GTC_REQUIRE(grad_weight->len >= g->m, GTC_ERR_ARG, "grad_weight is shorter than the edge bound");
+            GTC_REQUIRE(grad_weight->dtype == GTC_F64 || grad_weight->dtype == GTC_F32, GTC_ERR_ARG,
+                        "grad_weight: unknown dtype");
+            in.grad_w = grad_weight->ptr;
+            in.grad_w_dtype = grad_weight->dtype;
+        }
+        if (grad_pers && grad_pers->ptr) {
+            GTC_REQUIRE(grad_pers->len >= g->n, GTC_ERR_ARG, "grad_pers is shorter than the vertex bound");
+            GTC_REQUIRE(grad_pers->dtype == GTC_F64 || grad_pers->dtype == GTC_F32, GTC_ERR_ARG,
+                        "grad_pers: unknown dtype");
+            in.grad_p = grad_pers->ptr;
+            in.grad_p_dtype = grad_pers->dtype;
+        }
+        GTC_REQUIRE(!std::isnan(damping), GTC_ERR_ARG, "damping is NaN");
+        GTC_REQUIRE(!opt || opt->precision == GTC_PREC_F32, GTC_ERR_ARG,
+                    "the PageRank adjoint runs in GTC_PREC_F32");
+        in.damping = damping;
+        in.timing = opt && opt->timing;
+        gtc_result r{};
+        gtc::pagerank_adjoint(g, view, in, &r, stream_of(g, opt));
+        if (result) *result = r;
+    });
+}
+
+int gtc_pagerank_adjoint(gtc_graph* g, const gtc_view* view, const double* weight,
+                         uint64_t weight_len, const double* pers, uint64_t pers_len, double damping,
+                         const gtc_power_iteration* params, const double* pi, const double* grad_pi,
+                         double* grad_weight, double* grad_pers, const gtc_options* opt,
+                         gtc_result* result) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        GTC_REQUIRE(!weight || weight_len >= g->m, GTC_ERR_ARG, "weight map is shorter than the edge bound");
+        GTC_REQUIRE(!pers || pers_len >= g->n, GTC_ERR_ARG,
+                    "personalisation map is shorter than the vertex bound");
+        GTC_REQUIRE((pi && grad_pi) || g->n == 0, GTC_ERR_ARG, "pi / grad_pi is NULL");
+        cudaStream_t s = stream_of(g, opt);
+        const uint32_t n = g->n, m = g->m;
+        DevBuf<double> dw, dp, dpi(n, s), dg(n, s), dgw, dgp;
+        if (weight) {
+            dw.alloc(m, s);
+            if (m) GTC_CUDA(cudaMemcpyAsync(dw.get(), weight, (size_t)m * 8, cudaMemcpyHostToDevice, s));
+        }
+        if (pers) {
+            dp.alloc(n, s);
+            if (n) GTC_CUDA(cudaMemcpyAsync(dp.get(), pers, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+        }
+        if (n) {
+            GTC_CUDA(cudaMemcpyAsync(dpi.get(), pi, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+            GTC_CUDA(cudaMemcpyAsync(dg.get(), grad_pi, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+        }
+        if (grad_weight) dgw.alloc(m, s);
+        if (grad_pers) dgp.alloc(n, s);
+        gtc_dvec vw{dw.get(), m, GTC_F64, 0}, vp{dp.get(), n, GTC_F64, 0};
+        gtc_dvec vpi{dpi.get(), n, GTC_F64, 0}, vg{dg.get(), n, GTC_F64, 0};
+        gtc_dvec vgw{dgw.get(), m, GTC_F64, 0}, vgp{dgp.get(), n, GTC_F64, 0};
+        gtc_options o = opt ? *opt : gtc_options{};
+        o.stream = (void*)s;
+        const int st = gtc_pagerank_adjoint_device(g, view, weight ? &vw : nullptr,
+                                                   pers ? &vp : nullptr, damping, params, &vpi, &vg,
+                                                   grad_weight ? &vgw : nullptr,
+                                                   grad_pers ? &vgp : nullptr, &o, result);
+        if (st != GTC_OK) throw Error{st, gtc_last_error()};
+        if (grad_weight && m)
+            GTC_CUDA(cudaMemcpyAsync(grad_weight, dgw.get(), (size_t)m * 8, cudaMemcpyDeviceToHost, s));
+        if (grad_pers && n)
+            GTC_CUDA(cudaMemcpyAsync(grad_pers, dgp.get(), (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
 }  // extern "C"

@@ -872,4 +872,209 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
     g->launches += L;
 }
 
+// --------------------------------------------------------------------------
+// the PageRank adjoint
+// --------------------------------------------------------------------------
+//
+// Forward fixed point pi = (1-d) p + d (A pi + p (s . pi)), A[t][s] = w_e/deg_s
+// for deg_s != 0 (sinks s contribute through the dangling mass only).  For
+// L(pi) with g = dL/dpi the adjoint lambda solves
+//     lambda = g + d (A^T lambda + s (p . lambda)),
+// and (A^T lambda)_s = sum over s's out-edges of (w_e/deg_s) lambda_t, a pull
+// over the out-halves.  By the implicit-function theorem only the converged
+// pi is needed:
+//     dL/dp_v = lambda_v ((1-d) + d (s . pi))
+//     dL/dw_e = d (pi_s/deg_s) (lambda_t - (A^T lambda)_s)   (e: s->t, deg_s != 0)
+// (the second term comes from deg_s depending on w_e).  Edges out of a vertex
+// whose weighted degree is 0 get 0 (the map is not differentiable there).
+
+// ptl = p . lambda (deterministic block fold: b = sum)
+__global__ void __launch_bounds__(PR_NT) k_dot(uint32_t n, const float* __restrict__ p,
+                                              float uniform, const float* __restrict__ x,
+                                              Fold2 f) {
+    Kahan acc;
+    for (size_t v = (size_t)blockIdx.x * PR_NT + threadIdx.x; v < n;
+         v += (size_t)gridDim.x * PR_NT)
+        acc.add(__fmul_rn(p ? p[v] : uniform, x[v]));
+    block_fold2<PR_NT>(0.0, (double)acc.s + (double)acc.c, f);
+}
+
+// grad_p[v] = lambda[iperm v] * c (original labels)
+__global__ void k_grad_pers(uint32_t n, const uint32_t* __restrict__ iperm,
+                            const float* __restrict__ lam, const double* __restrict__ psink_pi,
+                            double one_minus_d, double d, void* __restrict__ out, int dt) {
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const double c = one_minus_d + d * (*psink_pi);
+    const double gv = (double)lam[iperm[v]] * c;
+    if (dt == GTC_F64)
+        ((double*)out)[v] = gv;
+    else
+        ((float*)out)[v] = (float)gv;
+}
+
+// grad_w over the out-half entries: thread per entry, its row by binary search
+__global__ void k_grad_w(uint32_t n, uint32_t m, const uint32_t* __restrict__ off,
+                         const uint32_t* __restrict__ other, const uint32_t* __restrict__ eid,
+                         const float* __restrict__ y, const float* __restrict__ lam,
+                         const float* __restrict__ atl, const double* __restrict__ deg, float d,
+                         void* __restrict__ out, int dt) {
+    size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m) return;
+    uint32_t lo = 0, hi = n;  // last row with off[row] <= p
+    while (hi - lo > 1) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (off[mid] <= (uint32_t)p)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    const uint32_t s = lo;
+    float gw = 0.f;
+    if (deg[s] != 0.0) gw = __fmul_rn(__fmul_rn(d, y[s]), __fsub_rn(lam[other[p]], atl[s]));
+    const uint32_t e = eid[p];
+    if (dt == GTC_F64)
+        ((double*)out)[e] = (double)gw;
+    else
+        ((float*)out)[e] = gw;
+}
+
+void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc_result* res,
+                      cudaStream_t s) {
+    uint64_t L = 0, SL = 0;
+    const unsigned TB = 256;
+    GTC_REQUIRE(!vw || (!vw->vmask && !vw->emask), GTC_ERR_ARG,
+                "the PageRank adjoint supports the graph and its reversal, not filtered views");
+    // the forward view: degrees, sinks, pi
+    SolveIn fin{};
+    fin.weight = in.weight;
+    fin.pers = in.pers;
+    fin.x = const_cast<void*>(in.pi.p);
+    fin.x_dtype = in.pi.dtype;
+    fin.had = g->n;  // pi is the seed: x64 = pi (internal labels)
+    Prep P;
+    prepare(g, vw, fin, true, P, s, &L);
+    const uint32_t n = P.view.n;
+    const double d = in.damping;
+    DevBuf<float> invdeg(n, s), pers32, g32(n, s), pi32(n, s), ypi((size_t)n + 1, s);
+    if (n) {
+        k_invdeg_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.deg.get(), invdeg.get());
+        k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.x64.get(), GTC_F64, nullptr, pi32.get());
+        k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, in.gpi.p, in.gpi.dtype, g->perm.get(),
+                                                          g32.get());
+        GTC_LAUNCHED();
+        L += 3;
+    }
+    if (in.pers.present() && n) {
+        pers32.alloc(n, s);
+        k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, in.pers.p, in.pers.dtype, g->perm.get(),
+                                                          pers32.get());
+        GTC_LAUNCHED();
+        L++;
+    }
+    const unsigned nb = persistent_blocks(n);
+    FoldBufs fb(nb, s);
+    double* dp = fb.out.get();  // [1] dangling mass of pi, [3] p . lambda0
+    // y = pi / deg and the dangling mass of pi
+    k_pr_prime<<<nb, PR_NT, 0, s>>>(n, pi32.get(), invdeg.get(), P.sink.get(), ypi.get(),
+                                   fb.fold(dp + 2, dp + 1));
+    GTC_LAUNCHED();
+    L++;
+
+    // the adjoint pulls over the forward view's out-halves: the reversed view
+    gtc_view rv{};
+    rv.reversed = (vw && vw->reversed) ? 0 : 1;
+    View av;
+    av.prepare(g, &rv, s, &L);
+    Units local;
+    Units* U = pull_units(g, av, local, s);
+    const bool W = in.weight.present();
+    DevBuf<float> wpull;
+    if (W && av.m_pull) {
+        wpull.alloc(av.m_pull, s);
+        k_gather_w<float><<<grid_for(av.m_pull, 256, 1u << 30), 256, 0, s>>>(
+            av.m_pull, av.pull_eid, in.weight.p, in.weight.dtype, wpull.get());
+        GTC_LAUNCHED();
+        L++;
+    }
+    DevBuf<float> lam0((size_t)n + 1, s), lam1((size_t)n + 1, s), atl((size_t)n + 1, s);
+    GTC_CUDA(cudaMemsetAsync(lam0.get() + n, 0, sizeof(float), s));
+    GTC_CUDA(cudaMemsetAsync(lam1.get() + n, 0, sizeof(float), s));
+    if (n) GTC_CUDA(cudaMemcpyAsync(lam0.get(), g32.get(), (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    FoldBufs fd(nb, s);
+    k_dot<<<nb, PR_NT, 0, s>>>(n, pers32.get(), (float)P.uniform, lam0.get(),
+                              fd.fold(fd.out.get() + 2, fd.out.get() + 3));
+    GTC_LAUNCHED();
+    L++;
+    FoldBufs fs(1, s);
+    double* dq = fs.out.get();  // [0] delta, [1] p . lambda of the current iterate
+    GTC_CUDA(cudaMemcpyAsync(dq + 1, fd.out.get() + 3, sizeof(double), cudaMemcpyDeviceToDevice, s));
+
+    SweepArgs A{};
+    set_schedule(A, *U, av);
+    DevBuf<float> swt = sliced_weights(*U, fin, s, &L);
+    A.sw = swt.get();
+    A.w = wpull.get();
+    A.invdeg = invdeg.get();
+    A.sink = P.sink.get();
+    A.pers = pers32.get();
+    A.gvec = g32.get();
+    A.uniform = (float)P.uniform;
+    A.one_minus_d = (float)(1.0 - d);
+    A.d = (float)d;
+    A.psink = dq + 1;
+    A.ticket = fs.ticket.get();
+    A.out = dq;
+    A.ynext = atl.get();
+    float *lc = lam0.get(), *ln = lam1.get();
+    A.x = lc, A.prev = lc, A.next = ln;
+    const int var = tuned_variant<MODE_ADJOINT>(*U, A, W, s, &L);
+    GTC_CUDA(cudaMemcpyAsync(dq + 1, fd.out.get() + 3, sizeof(double), cudaMemcpyDeviceToDevice, s));
+
+    const uint64_t max_iter = in.params.max_iter;
+    const double eps = in.params.epsilon;
+    uint64_t iter = 0;
+    double delta = eps + 1.0, sweep_ms = 0.0;
+    Timer total(s), sw(s);
+    total.start();
+    while (delta >= eps) {
+        A.x = lc, A.prev = lc, A.next = ln;
+        if (in.timing) sw.start();
+        launch_sweep<MODE_ADJOINT>(var, A, W, s);
+        if (in.timing) sw.stop();
+        L++;
+        SL++;
+        GTC_CUDA(cudaMemcpyAsync(&delta, dq, sizeof(double), cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+        if (in.timing) sweep_ms += sw.ms();
+        std::swap(lc, ln);
+        iter++;
+        if (max_iter > 0 && iter == max_iter) break;
+    }
+    total.stop();
+    res->device_ms = total.ms();
+    // gradients
+    if (in.grad_p && n) {
+        k_grad_pers<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->iperm.get(), lc, dp + 1, 1.0 - d,
+                                                             d, in.grad_p, in.grad_p_dtype);
+        GTC_LAUNCHED();
+        L++;
+    }
+    if (in.grad_w && av.m_pull) {
+        k_grad_w<<<grid_for(av.m_pull, TB, 1u << 30), TB, 0, s>>>(
+            n, av.m_pull, av.pull_off, av.pull_other, av.pull_eid, ypi.get(), lc, atl.get(),
+            P.deg.get(), (float)d, in.grad_w, in.grad_w_dtype);
+        GTC_LAUNCHED();
+        L++;
+    }
+    GTC_CUDA(cudaStreamSynchronize(s));
+    res->iterations = iter;
+    res->last_delta = iter ? delta : 0.0;
+    res->eigenvalue = 0.0;
+    res->launches = L;
+    res->sweep_ms = sweep_ms;
+    res->sweep_launches = SL;
+    g->launches += L;
+}
+
 }  // namespace gtc

@@ -117,7 +117,7 @@ struct Units {
     DevBuf<uint32_t> seid;       // sliced entries: edge id (0xFFFFFFFF pads)
     uint32_t n_units = 0, n_long = 0, n_chunks = 0, n_med = 0, n_slices = 0;
     uint32_t n_sliced = 0;       // sliced entries including padding
-    int variant[2][2] = {{-1, -1}, {-1, -1}};  // tuned kernel variant [mode][weighted]
+    int variant[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};  // tuned kernel variant [mode][weighted]
     bool built = false;
 };
 
@@ -172,7 +172,23 @@ __device__ __forceinline__ double ld_any(const void* p, int dtype, size_t i) {
     return dtype == GTC_F64 ? ((const double*)p)[i] : (double)((const float*)p)[i];
 }
 
+// Inputs of the PageRank adjoint (device vectors, original labels).
+struct AdjointIn {
+    DVec weight, pers;           // as the forward solve
+    double damping = 0.85;
+    gtc_power_iteration params;  // epsilon / max_iter of the adjoint iteration
+    DVec pi;                     // the converged forward result
+    DVec gpi;                    // dL/dpi
+    void* grad_w = nullptr;      // out: dL/dw by EdgeId (may be null)
+    int grad_w_dtype = GTC_F64;
+    void* grad_p = nullptr;      // out: dL/dpers by vertex (may be null)
+    int grad_p_dtype = GTC_F64;
+    bool timing = false;
+};
+
 // solves (gtc_centrality.cu)
+void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc_result* res,
+                      cudaStream_t s);
 void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* res,
               cudaStream_t s);
 void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* res,

@@ -48,7 +48,11 @@ constexpr uint32_t UNIT_SLICES = 3;  // slice y
 void build_units(const uint32_t* d_off, const uint32_t* d_other, const uint32_t* d_eid,
                  uint32_t n, cudaStream_t s, Units& u);
 
-enum SweepMode { MODE_PAGERANK = 0, MODE_EIGEN = 1 };
+// PAGERANK: the pull sweep of pagerank_with.  EIGEN: the unnormalised sweep
+// of eigenvector.  ADJOINT: one step of the adjoint fixed point
+// lambda <- g + d (A^T lambda + s (p^T lambda)) of PageRank, pulled over the
+// out-halves (A^T lambda at s is a sum over s's out-edges).
+enum SweepMode { MODE_PAGERANK = 0, MODE_EIGEN = 1, MODE_ADJOINT = 2 };
 
 struct SweepArgs {
     // schedule
@@ -77,9 +81,10 @@ struct SweepArgs {
     float* __restrict__ ynext;          // PageRank only
     const float* __restrict__ invdeg;   // PageRank only
     const uint8_t* __restrict__ sink;   // PageRank only
-    const float* __restrict__ pers;     // PageRank only (null = uniform)
+    const float* __restrict__ pers;     // PageRank / adjoint (null = uniform)
+    const float* __restrict__ gvec;     // adjoint: dL/dpi
     float uniform, one_minus_d, d;
-    const double* psink;                // PageRank: dangling mass of prev
+    const double* psink;                // PageRank: dangling mass of prev; adjoint: p . prev
     // reduction: every item's terms, folded by the last CTA
     unsigned* ticket;
     double* out;  // [a, b]
@@ -125,6 +130,16 @@ __device__ __forceinline__ void sweep_row(const SweepArgs& A, uint32_t v, float 
         A.ynext[v] = __fmul_rn(nv, __ldcs(A.invdeg + v));
         ta = fabsf(__fsub_rn(nv, __ldcs(A.prev + v)));
         tb = __ldcs(A.sink + v) ? nv : 0.f;
+    } else if (MODE == MODE_ADJOINT) {
+        // sum = sum over v's out-edges of w * lambda[t]; A^T lambda = sum / deg
+        const float at = __fmul_rn(__ldcs(A.invdeg + v), sum);
+        const float dn = __ldcs(A.sink + v) ? __fadd_rn(at, psink) : at;
+        const float nv = __fadd_rn(__ldcs(A.gvec + v), __fmul_rn(A.d, dn));
+        __stcs(A.next + v, nv);
+        A.ynext[v] = at;  // kept for the weight gradient
+        ta = fabsf(__fsub_rn(nv, __ldcs(A.prev + v)));
+        const float pv = A.pers ? __ldcs(A.pers + v) : A.uniform;
+        tb = __fmul_rn(pv, nv);  // next sweep's p . lambda
     } else {
         A.next[v] = sum;
         ta = __fmul_rn(sum, sum);
@@ -154,7 +169,7 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
     __shared__ double fa[SP_FOLD], fb[SP_FOLD];
     __shared__ bool flag;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const float psink = MODE == MODE_PAGERANK ? (float)*A.psink : 0.f;
+    const float psink = MODE != MODE_EIGEN ? (float)*A.psink : 0.f;
     if (HOT) {
         const float4* src = reinterpret_cast<const float4*>(A.x);
         float4* dst = reinterpret_cast<float4*>(hot);

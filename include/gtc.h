@@ -205,6 +205,32 @@ int gtc_eigenvector_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* w
                            const gtc_power_iteration* params, gtc_dvec* x, uint64_t x_had,
                            const gtc_options* opt, gtc_result* result);
 
+/* ---- gradients ---------------------------------------------------------
+ *
+ * The adjoint of PageRank (no counterpart in the reference, which has no
+ * differentiation): for a scalar L(pi) of the converged PageRank pi, with
+ * grad_pi = dL/dpi, solve lambda = grad_pi + d (A^T lambda + s (p . lambda))
+ * (A^T pulled over the out-halves, s the dangling vertices) to epsilon, then
+ *   grad_pers[v]   = lambda_v ((1-d) + d (s . pi))
+ *   grad_weight[e] = d (pi_s / deg_s) (lambda_t - (A^T lambda)_s)   e: s -> t
+ * (0 for edges out of a vertex of zero weighted degree).  Only the converged
+ * pi is used (implicit-function theorem): no iterate history is kept.
+ * weight / pers / damping are the forward solve's (NULL = Unity / uniform).
+ * GTC_PREC_F32 only; plain or reversed views.  grad_weight (edge bound) and
+ * grad_pers (vertex bound) may be NULL to skip them. */
+int gtc_pagerank_adjoint(gtc_graph* g, const gtc_view* view, const double* weight,
+                         uint64_t weight_len, const double* pers, uint64_t pers_len, double damping,
+                         const gtc_power_iteration* params, const double* pi, const double* grad_pi,
+                         double* grad_weight, double* grad_pers, const gtc_options* opt,
+                         gtc_result* result);
+
+/* As gtc_pagerank_adjoint with every vector in device memory (FP32 or FP64). */
+int gtc_pagerank_adjoint_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* weight,
+                                const gtc_dvec* pers, double damping,
+                                const gtc_power_iteration* params, const gtc_dvec* pi,
+                                const gtc_dvec* grad_pi, gtc_dvec* grad_weight, gtc_dvec* grad_pers,
+                                const gtc_options* opt, gtc_result* result);
+
 /* ---- PageRank without any allocation ------------------------------------
  *
  * No counterpart in the reference: an addition for callers that cannot
