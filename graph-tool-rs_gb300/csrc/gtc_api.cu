@@ -434,4 +434,65 @@ int gtc_pagerank_adjoint(gtc_graph* g, const gtc_view* view, const double* weigh
     });
 }
 
+int gtc_ppr_batch_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* weight, uint32_t B,
+                         const uint64_t* seed_off, const uint32_t* seed_vertices,
+                         const double* seed_values, double damping,
+                         const gtc_power_iteration* params, gtc_dvec* ranks, uint64_t* iters,
+                         const gtc_options* opt, gtc_result* result) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        PprIn in{};
+        check_params(g, params, in.params);
+        in.weight = dvec_in(weight, g->m, "weight");
+        GTC_REQUIRE(seed_off && (seed_off[B] == 0 || seed_vertices), GTC_ERR_ARG,
+                    "seed_off / seed_vertices is NULL");
+        GTC_REQUIRE(iters, GTC_ERR_ARG, "iters is NULL");
+        GTC_REQUIRE(ranks && (ranks->ptr || g->n == 0), GTC_ERR_ARG, "ranks is NULL");
+        GTC_REQUIRE(ranks->len >= (uint64_t)B * g->n, GTC_ERR_ARG, "ranks holds fewer than B x n entries");
+        GTC_REQUIRE(ranks->dtype == GTC_F64 || ranks->dtype == GTC_F32, GTC_ERR_ARG, "ranks: unknown dtype");
+        GTC_REQUIRE(!std::isnan(damping), GTC_ERR_ARG, "damping is NaN");
+        GTC_REQUIRE(!opt || opt->precision == GTC_PREC_F32, GTC_ERR_ARG,
+                    "batched personalised PageRank runs in GTC_PREC_F32");
+        in.B = B;
+        in.seed_off = seed_off;
+        in.seed_vertices = seed_vertices;
+        in.seed_values = seed_values;
+        in.damping = damping;
+        in.out = ranks->ptr;
+        in.out_dtype = ranks->dtype;
+        in.iters = iters;
+        gtc_result r{};
+        gtc::ppr_batch(g, view, in, &r, stream_of(g, opt));
+        if (result) *result = r;
+    });
+}
+
+int gtc_ppr_batch(gtc_graph* g, const gtc_view* view, const double* weight, uint64_t weight_len,
+                  uint32_t B, const uint64_t* seed_off, const uint32_t* seed_vertices,
+                  const double* seed_values, double damping, const gtc_power_iteration* params,
+                  double* ranks, uint64_t* iters, const gtc_options* opt, gtc_result* result) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        GTC_REQUIRE(!weight || weight_len >= g->m, GTC_ERR_ARG, "weight map is shorter than the edge bound");
+        GTC_REQUIRE(ranks || g->n == 0 || B == 0, GTC_ERR_ARG, "ranks is NULL");
+        cudaStream_t s = stream_of(g, opt);
+        const uint32_t n = g->n, m = g->m;
+        DevBuf<double> dw, dr((size_t)B * n, s);
+        if (weight) {
+            dw.alloc(m, s);
+            if (m) GTC_CUDA(cudaMemcpyAsync(dw.get(), weight, (size_t)m * 8, cudaMemcpyHostToDevice, s));
+        }
+        gtc_dvec vw{dw.get(), m, GTC_F64, 0}, vr{dr.get(), (uint64_t)B * n, GTC_F64, 0};
+        gtc_options o = opt ? *opt : gtc_options{};
+        o.stream = (void*)s;
+        const int st = gtc_ppr_batch_device(g, view, weight ? &vw : nullptr, B, seed_off,
+                                            seed_vertices, seed_values, damping, params, &vr, iters,
+                                            &o, result);
+        if (st != GTC_OK) throw Error{st, gtc_last_error()};
+        if ((size_t)B * n)
+            GTC_CUDA(cudaMemcpyAsync(ranks, dr.get(), (size_t)B * n * 8, cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
 }  // extern "C"

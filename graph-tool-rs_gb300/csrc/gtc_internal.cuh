@@ -186,6 +186,22 @@ struct AdjointIn {
     bool timing = false;
 };
 
+// Inputs of a batch of personalised PageRanks (gtc_ppr.cu).
+struct PprIn {
+    DVec weight;                      // by EdgeId, device, or absent (Unity)
+    uint32_t B = 0;                   // personalisation vectors
+    const uint64_t* seed_off = nullptr;       // host, B + 1
+    const uint32_t* seed_vertices = nullptr;  // host, original labels
+    const double* seed_values = nullptr;      // host, or null: 1/|set|
+    double damping = 0.85;
+    gtc_power_iteration params;
+    void* out = nullptr;              // device [B][n] ranks (original labels)
+    int out_dtype = GTC_F64;
+    uint64_t* iters = nullptr;        // host, B: sweeps of every column
+};
+void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* res,
+               cudaStream_t s);
+
 // solves (gtc_centrality.cu)
 void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc_result* res,
                       cudaStream_t s);

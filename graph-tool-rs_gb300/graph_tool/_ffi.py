@@ -97,6 +97,13 @@ SIGNATURES = {
     "gtc_eigenvector_device": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(DVec),
                                          C.POINTER(PowerIteration), C.POINTER(DVec), C.c_uint64,
                                          C.POINTER(Options), C.POINTER(Result)]),
+    "gtc_ppr_batch": (C.c_int, [C.c_void_p, C.POINTER(View), f64p, C.c_uint64, C.c_uint32, u64p,
+                                u32p, f64p, C.c_double, C.POINTER(PowerIteration), f64p, u64p,
+                                C.POINTER(Options), C.POINTER(Result)]),
+    "gtc_ppr_batch_device": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(DVec), C.c_uint32,
+                                       u64p, u32p, f64p, C.c_double, C.POINTER(PowerIteration),
+                                       C.POINTER(DVec), u64p, C.POINTER(Options),
+                                       C.POINTER(Result)]),
     "gtc_pagerank_adjoint": (C.c_int, [C.c_void_p, C.POINTER(View), f64p, C.c_uint64, f64p,
                                        C.c_uint64, C.c_double, C.POINTER(PowerIteration), f64p,
                                        f64p, f64p, f64p, C.POINTER(Options), C.POINTER(Result)]),

@@ -205,6 +205,30 @@ int gtc_eigenvector_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* w
                            const gtc_power_iteration* params, gtc_dvec* x, uint64_t x_had,
                            const gtc_options* opt, gtc_result* result);
 
+/* ---- batched personalised PageRank -------------------------------------
+ *
+ * B personalised PageRanks over one edge stream (an SpMM over B right-hand
+ * sides; the reference calls pagerank_with, centrality.rs:261-384, once per
+ * vector).  Vector b's personalisation is its seed set
+ * seed_vertices[seed_off[b] .. seed_off[b+1]) with seed_values (NULL:
+ * 1/|set| each); each column starts from its personalisation (a fresh map,
+ * centrality.rs:198-205) and stops at the first sweep whose L1 change is
+ * below params->epsilon (or at max_iter); iters[b] receives its sweep count.
+ * ranks is [B][n] (row b = vector b, by vertex index).  1 <= B <= 512.
+ * GTC_PREC_F32; plain or reversed views.  Host arrays except as named. */
+int gtc_ppr_batch(gtc_graph* g, const gtc_view* view, const double* weight, uint64_t weight_len,
+                  uint32_t B, const uint64_t* seed_off, const uint32_t* seed_vertices,
+                  const double* seed_values, double damping, const gtc_power_iteration* params,
+                  double* ranks, uint64_t* iters, const gtc_options* opt, gtc_result* result);
+
+/* As gtc_ppr_batch with the weights and the [B][n] ranks in device memory
+ * (the seed arrays and iters stay host arrays). */
+int gtc_ppr_batch_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* weight, uint32_t B,
+                         const uint64_t* seed_off, const uint32_t* seed_vertices,
+                         const double* seed_values, double damping,
+                         const gtc_power_iteration* params, gtc_dvec* ranks, uint64_t* iters,
+                         const gtc_options* opt, gtc_result* result);
+
 /* ---- gradients ---------------------------------------------------------
  *
  * The adjoint of PageRank (no counterpart in the reference, which has no

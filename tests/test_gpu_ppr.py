@@ -1,0 +1,76 @@
+"""Batched personalised PageRank (one SpMM over B right-hand sides) against
+the oracle's pagerank_with, one call per seed set (the reference's way)."""
+import numpy as np
+import pytest
+
+import _cases as K
+
+pytestmark = pytest.mark.gpu
+
+
+def _seed_sets(n, B, rng, max_size=8):
+    sets = []
+    for _ in range(B):
+        k = int(rng.integers(1, max_size + 1))
+        sets.append(rng.choice(n, k, replace=False))
+    return sets
+
+
+def _check(oracle, gtc, n, src, tgt, B, weight=None, reversed=False, eps=1e-7, seed=1):
+    rng = np.random.default_rng(seed)
+    sets = _seed_sets(n, B, rng)
+    g = gtc.Graph()
+    g.add_vertex(n)
+    g.add_edges(src, tgt)
+    wm = None
+    if weight is not None:
+        wm = g.new_edge_property("double")
+        wm.a[:] = weight
+    ranks, iters = g.ppr_batch(sets, weight=wm, epsilon=eps, max_iter=1000, reversed=reversed)
+    og = oracle.Graph(n)
+    og.add_edge_arrays(src, tgt)
+    worst = 0.0
+    for b, st in enumerate(sets):
+        pers = np.zeros(n)
+        pers[st] = 1.0 / len(st)
+        want, it = og.pagerank(weight=weight, pers=pers, epsilon=eps, max_iter=1000, grain=4096,
+                               reversed=reversed)
+        err = np.abs(ranks[b] - want).sum() / np.abs(want).sum()
+        worst = max(worst, err)
+        assert err < 1e-6, (b, err, iters[b], it)
+        assert abs(int(iters[b]) - it) <= 3, (b, iters[b], it)
+    print(f"ppr batch B={B}: worst rel L1 {worst:.2e}")
+
+
+def test_ppr_batch_matches_separate_solves(oracle, gtc):
+    from graph_tool import synth
+    n, src, tgt, _ = synth.erdos_renyi_sinks(n=3000, m=24000)
+    _check(oracle, gtc, n, src, tgt, 37)
+
+
+def test_ppr_batch_padded_columns_weighted(oracle, gtc):
+    from graph_tool import synth
+    n, src, tgt = synth.rmat_cpu(11, edge_factor=8, seed=4)
+    w = np.random.default_rng(2).uniform(0.1, 1.0, src.size)
+    _check(oracle, gtc, n, src, tgt, 130, weight=w, seed=3)
+
+
+def test_ppr_batch_reversed_with_hubs(oracle, gtc):
+    # a hub with more in-edges than one warp row takes (a CTA row)
+    rng = np.random.default_rng(5)
+    n, m = 4000, 40000
+    src = rng.integers(0, n, m)
+    tgt = rng.integers(0, n, m)
+    tgt[: 6000] = 7
+    _check(oracle, gtc, n, src.astype(np.uint32), tgt.astype(np.uint32), 64, seed=6)
+    _check(oracle, gtc, n, src.astype(np.uint32), tgt.astype(np.uint32), 64, seed=7, reversed=True)
+
+
+def test_ppr_batch_rejects_bad_batches(gtc):
+    g = gtc.Graph()
+    g.add_vertex(3)
+    g.add_edge(0, 1)
+    with pytest.raises(ValueError):
+        g.ppr_batch([[0]] * 513)
+    with pytest.raises(IndexError):
+        g.ppr_batch([[5]])
