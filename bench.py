@@ -25,6 +25,17 @@ edges x sweeps / seconds / 1e9.
   cpu_baseline  the CPU oracle (a C restatement of the reference's f64
             path, all host threads) on the same graph, bounded to a few sweeps.
 
+Two more measurements ride on the same line (skipped with --no-secondary):
+
+  adjoint   gradient of L = c . pi (c ~ N(0,1)) with respect to FP32 edge
+            weights U(0.1, 1) and a Dirichlet(1) personalisation on the same
+            RMAT-24 graph, forward and adjoint epsilon 1e-7: the adjoint's
+            time over the forward solve's.
+  ppr_batch RMAT-22 (4,194,304 vertices, edge factor 16, deduplicated),
+            B = 256 personalisation vectors, each uniform over a seed set of
+            1-64 vertices, epsilon 1e-6: solves per second batched (one SpMM
+            sweep for all columns) and as 256 sequential single solves.
+
 ``--impl reference`` times that CPU restatement alone (the reference itself
 is Rust and cannot be built here).  Inputs are larger than L2 (the graph's
 index arrays alone are ~1 GB), so no flush runs between steps.
@@ -175,6 +186,145 @@ def run_cpu(g, m, w_np, eps, sweeps, threads):
     return m * it / dt / 1e9, dt, it
 
 
+def _events_ms(fn, stream, reps=1):
+    import torch
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    out = [fn() for _ in range(reps)]
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps, out
+
+
+def adjoint_section(L, h, n, m, device, stream, wl):
+    """Adjoint / forward time on the headline graph, weighted and personalised."""
+    import torch
+    from graph_tool import _ffi, synth_gpu
+    u = synth_gpu._unit(synth_gpu.splitmix(7001, 0, m, device))
+    w = (0.1 + 0.9 * u).to(torch.float32)
+    e = -torch.log1p(-synth_gpu._unit(synth_gpu.splitmix(7002, 0, n, device)))
+    pers = (e / e.sum()).to(torch.float32)                       # Dirichlet(1)
+    u1 = synth_gpu._unit(synth_gpu.splitmix(7003, 0, n, device)).clamp_min(1e-300)
+    u2 = synth_gpu._unit(synth_gpu.splitmix(7004, 0, n, device))
+    c = (torch.sqrt(-2 * torch.log(u1)) * torch.cos(6.283185307179586 * u2)).to(torch.float32)
+    pi = torch.empty(n, dtype=torch.float32, device=device)
+    gw = torch.empty(m, dtype=torch.float32, device=device)
+    gp = torch.empty(n, dtype=torch.float32, device=device)
+    params = _ffi.PowerIteration(1e-7, MAX_ITER, n, (n + 4095) // 4096)
+    opt = _ffi.Options(_ffi.GTC_PREC_F32, 0, C.c_void_p(stream.cuda_stream), 0, 0)
+    wv, pv, piv = _ffi.DVec.of(w), _ffi.DVec.of(pers), _ffi.DVec.of(pi)
+    cv, gwv, gpv = _ffi.DVec.of(c), _ffi.DVec.of(gw), _ffi.DVec.of(gp)
+
+    def fwd():
+        r = _ffi.Result()
+        _ffi.check(L.gtc_pagerank_device(h, None, C.byref(wv), C.byref(pv), DAMPING,
+                                         C.byref(params), C.byref(piv), 0, C.byref(opt),
+                                         C.byref(r)))
+        return r.iterations
+
+    def adj():
+        r = _ffi.Result()
+        _ffi.check(L.gtc_pagerank_adjoint_device(h, None, C.byref(wv), C.byref(pv), DAMPING,
+                                                 C.byref(params), C.byref(piv), C.byref(cv),
+                                                 C.byref(gwv), C.byref(gpv), C.byref(opt),
+                                                 C.byref(r)))
+        return r.iterations
+
+    fwd(), adj()  # warm-up (first calls build the reversed schedule and tune)
+    t_f, it_f = _events_ms(fwd, stream, 3)
+    t_a, it_a = _events_ms(adj, stream, 3)
+    return {"workload": "rmat24, FP32 weights U(0.1,1), Dirichlet(1) pers, L = c.pi, c ~ N(0,1)",
+            "forward_ms": t_f, "adjoint_ms": t_a, "adjoint_over_forward": t_a / t_f,
+            "forward_sweeps": it_f[0], "adjoint_sweeps": it_a[0], "epsilon": 1e-7}
+
+
+def ppr_section(L, device, stream, B=256, sequential=True, scale=22):
+    """Batched personalised PageRank vs B sequential single solves, RMAT-22."""
+    import numpy as np
+    import torch
+    from graph_tool import _ffi, synth_gpu
+    n, src, tgt = synth_gpu.rmat(scale, 16, seed=3, device=device)
+    m = int(src.numel())
+    torch.cuda.synchronize()
+    h = C.c_void_p()
+    _ffi.check(L.gtc_graph_create_device(n, m, C.c_void_p(src.data_ptr()),
+                                         C.c_void_p(tgt.data_ptr()),
+                                         C.c_void_p(stream.cuda_stream), C.byref(h)))
+    _ffi.check(L.gtc_graph_set_stream(h, C.c_void_p(stream.cuda_stream)))
+    del src, tgt
+    torch.cuda.empty_cache()
+    rng = np.random.default_rng(22)
+    sizes = rng.integers(1, 65, B)
+    sets = [rng.choice(n, k, replace=False) for k in sizes]
+    off = np.zeros(B + 1, np.uint64)
+    off[1:] = np.cumsum(sizes)
+    verts = np.ascontiguousarray(np.concatenate(sets), dtype=np.uint32)
+    iters = np.zeros(B, np.uint64)
+    eps = 1e-6
+    params = _ffi.PowerIteration(eps, MAX_ITER, n, (n + 4095) // 4096)
+    opt = _ffi.Options(_ffi.GTC_PREC_F32, 0, C.c_void_p(stream.cuda_stream), 0, 0)
+    ranks = torch.empty(B * n, dtype=torch.float32, device=device)
+    rv = _ffi.DVec.of(ranks)
+
+    loop_ms = []
+
+    def batch():
+        r = _ffi.Result()
+        _ffi.check(L.gtc_ppr_batch_device(h, None, None, B, _ffi.ptr(off, _ffi.u64p),
+                                          _ffi.ptr(verts, _ffi.u32p), None, DAMPING,
+                                          C.byref(params), C.byref(rv),
+                                          _ffi.ptr(iters, _ffi.u64p), C.byref(opt), C.byref(r)))
+        loop_ms.append(r.device_ms)
+        return r.iterations
+
+    batch()
+    t_b, sw = _events_ms(batch, stream, 2)
+    batch_sweeps = iters.copy()
+    if not sequential:
+        _ffi.check(L.gtc_graph_destroy(h))
+        return {"batched_ms": t_b, "batched_loop_ms": loop_ms[-1], "batched_sweeps": int(sw[0]),
+                "column_sweeps_mean": float(batch_sweeps.mean())}
+    # B sequential single solves (personalisation vectors prepared beforehand)
+    pers = torch.zeros(B, n, dtype=torch.float32, device=device)
+    for b, st in enumerate(sets):
+        pers[b, torch.as_tensor(st, device=device)] = 1.0 / len(st)
+    one = torch.empty(n, dtype=torch.float32, device=device)
+    ov = _ffi.DVec.of(one)
+    pvs = [_ffi.DVec.of(pers[b]) for b in range(B)]
+    seq_sweeps = []
+
+    def seq():
+        for b in range(B):
+            r = _ffi.Result()
+            _ffi.check(L.gtc_pagerank_device(h, None, None, C.byref(pvs[b]), DAMPING,
+                                             C.byref(params), C.byref(ov), 0, C.byref(opt),
+                                             C.byref(r)))
+            seq_sweeps.append(r.iterations)
+        return 0
+
+    seq()  # warm-up
+    seq_sweeps.clear()
+    t_s, _ = _events_ms(seq, stream, 1)
+    # agreement of the two on a sample of columns
+    errs = []
+    for b in range(0, B, 37):
+        r = _ffi.Result()
+        _ffi.check(L.gtc_pagerank_device(h, None, None, C.byref(pvs[b]), DAMPING, C.byref(params),
+                                         C.byref(ov), 0, C.byref(opt), C.byref(r)))
+        a = ranks[b * n:(b + 1) * n].double()
+        errs.append(float((a - one.double()).abs().sum() / one.double().abs().sum()))
+    _ffi.check(L.gtc_graph_destroy(h))
+    return {"workload": f"rmat{scale} (n={n}, m={m}), B={B} seed sets of 1-64 vertices, eps {eps}",
+            "batched_solves_per_s": B / (t_b / 1e3), "sequential_solves_per_s": B / (t_s / 1e3),
+            "speedup_vs_sequential": t_s / t_b, "batched_ms": t_b, "sequential_ms": t_s,
+            "batched_sweeps": int(sw[0]), "batched_loop_ms": loop_ms[-1],
+            "column_sweeps_mean": float(batch_sweeps.mean()),
+            "sequential_sweeps_mean": float(np.mean(seq_sweeps)),
+            "max_rel_l1_batched_vs_single": max(errs)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -184,6 +334,7 @@ def main():
     ap.add_argument("--workload", default="rmat24", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-sweeps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     rank, world, local = env_rank()
@@ -347,6 +498,15 @@ def main():
                          f"{threads} OpenMP threads, {dt:.2f} s"}
         del g
 
+    secondary = {}
+    if not args.no_secondary and world == 1:
+        for name, fn in (("adjoint", adjoint_section), ("ppr_batch", ppr_section)):
+            try:
+                secondary[name] = fn(L, h, n, m, device, stream, wl) if name == "adjoint" else fn(L, device, stream)
+            except Exception as e:  # noqa: BLE001  (reported, the headline stands)
+                secondary[name] = {"error": repr(e)}
+            torch.cuda.empty_cache()
+
     if rank == 0:
         out = {
             "metric": "PageRank GTEPS", "value": value, "unit": "GTEPS", "n_gpus": world,
@@ -360,6 +520,7 @@ def main():
             "gpu_launches": int(launches), "sweep_launches": int(sweep_launches),
             "clocks": clk.summary(),
         }
+        out.update(secondary)
         print(json.dumps(out), flush=True)
     _ffi.check(L.gtc_graph_destroy(h))
     if world > 1:

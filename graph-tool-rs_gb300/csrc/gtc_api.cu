@@ -461,6 +461,7 @@ int gtc_ppr_batch_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* wei
         in.out = ranks->ptr;
         in.out_dtype = ranks->dtype;
         in.iters = iters;
+        in.timing = opt && opt->timing;
         gtc_result r{};
         gtc::ppr_batch(g, view, in, &r, stream_of(g, opt));
         if (result) *result = r;

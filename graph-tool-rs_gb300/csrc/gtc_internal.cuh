@@ -121,6 +121,19 @@ struct Units {
     bool built = false;
 };
 
+// Pull schedule of the batched personalised PageRank (gtc_ppr.cu): rows with
+// more in-edges than one chunk are cut into chunks, the rest are rows of
+// their own, heaviest first.
+struct PprSched {
+    // work items: the chunks {row, first entry, end entry, long row index},
+    // then the single rows {row, first entry, end entry, 0xFFFFFFFF} by
+    // descending in-degree (ties by index)
+    DevBuf<uint4> items;
+    DevBuf<uint4> longs;    // {row, first chunk, chunks, 0}
+    uint32_t n_items = 0, n_chunks = 0, n_long = 0;
+    bool built = false;
+};
+
 }  // namespace gtc
 
 struct gtc_graph {
@@ -137,6 +150,7 @@ struct gtc_graph {
     gtc::Halves out;  // CSR: out-halves (out_edges order)
     gtc::Halves in;   // CSC: in-halves (in_edges order, the pull order)
     gtc::Units units_in, units_out;  // pull schedules of the plain and reversed views
+    gtc::PprSched ppr_sched[2];      // batched schedules of the plain and reversed views
     uint64_t launches = 0;  // kernels this handle has launched (diagnostics)
 };
 
@@ -198,6 +212,7 @@ struct PprIn {
     void* out = nullptr;              // device [B][n] ranks (original labels)
     int out_dtype = GTC_F64;
     uint64_t* iters = nullptr;        // host, B: sweeps of every column
+    bool timing = false;
 };
 void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* res,
                cudaStream_t s);

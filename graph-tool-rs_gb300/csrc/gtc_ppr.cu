@@ -3,24 +3,43 @@
 // B personalisation vectors (seed sets) are solved together: pagerank_with
 // (crates/gt-algo/src/centrality.rs:261-384) for every column b, each from
 // its own start (a fresh map is seeded with pers_b, centrality.rs:198-205),
-// each stopping at the first sweep whose L1 change falls below epsilon.
+// each stopping at the first sweep whose L1 change falls below epsilon
+// (centrality.rs:372-381), its value the iterate of that sweep.
 //
-// Layout.  Z is [n x Bp] row-major (Bp = B rounded up to 128 columns): one
-// vertex's Bp values are contiguous, so the pull of an in-edge s -> v reads
-// Z[s][*] as whole 1 KB lines (B = 256) -- the gather of the single solve,
-// amortised over all columns.  Z[v][b] holds rank_b[v] / deg_v for a vertex
-// with out-edges and rank_b[v] itself for a sink (a sink is never gathered),
-// so one pair of ping-pong arrays carries both what is gathered and what the
-// L1 change is measured against.
+// Layout.  Z is [n x S] row-major, S = 32 * C slots (C = 1-4, 8, 12 or 16
+// lines of 128 bytes); a warp reads a row with C / V coalesced vector loads
+// of V floats per lane (Lanes<C>).  Z[v][j]
+// holds rank_b[v] / deg_v of the column b in slot j for a vertex with
+// out-edges, and rank_b[v] itself for a sink (a sink is never gathered).
 //
-// Schedule.  One warp per row (a lane owns Bp/32 consecutive columns, read
-// as float4), heaviest rows first; rows with more than PPR_LONG in-edges take
-// a whole CTA whose warps' compensated partials merge in warp order.  The
-// per-column FP64 change and dangling mass are folded per CTA and then, by
-// the last CTA, over CTAs in a fixed order: deterministic.  A column that
-// converged is frozen (carried unchanged) for the remaining sweeps.
+// Active columns only.  Columns converge at very different sweeps (for an
+// R-MAT graph and seed sets of 1-64 vertices the last column takes ~2.5x the
+// mean).  A column that converged is written to the output right away and
+// is dropped from the next sweep's output layout: the survivors are packed
+// into the lowest slots, so a sweep reads and writes ceil(active / 32) lines
+// per row, not B / 32.  The sweep that drops a column still gathers it (its
+// input layout is the previous sweep's output layout).
+//
+// Schedule.  Rows with more than PPR_CHUNK in-edges are cut into chunks of
+// PPR_CHUNK entries; the first kernel of a sweep runs every chunk (a warp
+// each, partials to memory) and every other row (a warp each, heaviest
+// first), the second merges each long row's chunk partials in chunk order and
+// finishes it.  Assignments are fixed strides and every fold runs in a fixed
+// order, so the results do not depend on timing.
+//
+// Latency.  A warp loads its next work item while it works on the current
+// one, and a row's epilogue inputs (degree, seeds, previous values) are
+// loaded before its gathers, so a row costs one index load plus its gather
+// rounds on the critical path.
+//
+// Precision.  Row sums are FP32 with Kahan compensation; the L1 change and
+// dangling mass per column are accumulated per warp with Kahan compensation
+// in FP32 and folded over warps and CTAs in FP64.  The per-row work stays off
+// the FP64 pipe (on this GPU a few FP64 operations per row cost more than the
+// row's gathers): degrees and their inverses are precomputed in FP32.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -31,37 +50,34 @@ namespace {
 
 constexpr int PPR_NT = 256;
 constexpr int PPR_WARPS = PPR_NT / 32;
-constexpr uint32_t PPR_LONG = 4096;   // rows with more in-edges take a whole CTA
-constexpr uint32_t PPR_MAXB = 512;    // largest batch
+constexpr uint32_t PPR_CHUNK = 1024;  // rows with more in-edges are cut into chunks
+constexpr uint32_t PPR_MAXB = 512;    // largest batch (16 lines per row)
+constexpr uint32_t PPR_NONE = 0xFFFFFFFFu;
 
 struct PprArgs {
-    uint32_t n, Bp;
-    const uint32_t* __restrict__ rows;   // warp rows, heaviest first
-    uint32_t n_rows;
-    const uint32_t* __restrict__ longs;  // CTA rows
+    uint32_t n, s_in, s_out;             // slots per row of zin and zout
+    const uint4* __restrict__ items;     // chunks, then single rows
+    uint32_t n_items, n_chunks;
+    const uint4* __restrict__ longs;     // {row, first chunk, chunks, 0}
     uint32_t n_long;
-    const uint32_t* __restrict__ off;
     const uint32_t* __restrict__ other;
     const float* __restrict__ w;         // pull-ordered weights or null
-    const float* __restrict__ zprev;     // [n][Bp]
-    float* __restrict__ znext;
-    const double* __restrict__ deg;
-    const uint8_t* __restrict__ sink;
+    const float* __restrict__ zin;       // [n][s_in]
+    float* __restrict__ zout;            // [n][s_out]
+    const float2* __restrict__ dinv;     // {FP32 out-degree, its inverse}; {-1, 0} for a sink
     const uint32_t* __restrict__ seed_off;  // per vertex: seeds [seed_off[v], seed_off[v+1])
     const uint2* __restrict__ seeds;        // {column, float bits of the value}
-    const uint8_t* __restrict__ frozen;     // per column
-    const double* __restrict__ psink;       // per column: dangling mass of prev
+    const uint32_t* __restrict__ col_in;    // [s_in] column in each input slot (PPR_NONE: empty)
+    const uint32_t* __restrict__ out_slot;  // [s_in] its output slot (PPR_NONE: not computed)
+    const float* __restrict__ psink;        // [s_in] dangling mass of zin per input slot
     float one_minus_d, d;
-    double* part;      // per CTA: 2*Bp doubles (delta[b], dangling mass[b])
-    unsigned* ticket;
-    double* out;       // 2*Bp: delta[b], then dangling mass of next [b]
+    float2* cpart;     // [n_chunks][s_in] compensated chunk partials (s, -c)
+    double* part;      // [CTAs of both kernels][2][s_in]
+    uint32_t part_base;
+    int* err;          // set when a bounded wait gave up
 };
 
-__device__ __forceinline__ float ldf(const float4& v, int k) {
-    return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
-}
-
-// Compensated accumulation of C columns (classic Kahan, value s - c).
+// Classic Kahan accumulation of C slots (value s - c).
 template <int C>
 struct Acc {
     float s[C], c[C];
@@ -75,206 +91,559 @@ struct Acc {
         c[k] = __fsub_rn(__fsub_rn(t, s[k]), y);
         s[k] = t;
     }
-    // a lane's C consecutive values of gathered row `src`
-    __device__ __forceinline__ void add_row(const float* __restrict__ z, uint32_t Bp, uint32_t src,
-                                            uint32_t c0, float w, bool weighted) {
-        const float4* r = reinterpret_cast<const float4*>(z + (size_t)src * Bp + c0);
+};
+
+// The slots of a lane.  A row of S = 32 * C slots is read by the warp as C
+// / V vector loads of V floats per lane (V = 4 when C is a multiple of 4, 2
+// when C is 2, else 1); the lane's q-th value is slot slot(lane, q).
+template <int C>
+struct Lanes {
+    static constexpr int V = C % 4 == 0 ? 4 : (C % 2 == 0 ? 2 : 1);
+    __device__ __forceinline__ static uint32_t slot(int lane, int q) {
+        return 32 * V * (q / V) + V * lane + (q % V);
+    }
+    // the lane's C values of a row (global memory through the read-only
+    // path, or shared memory)
+    template <bool GLOBAL>
+    __device__ __forceinline__ static void load(const float* row, int lane, float (&x)[C]) {
 #pragma unroll
-        for (int q = 0; q < C / 4; ++q) {
-            const float4 a = __ldg(r + q);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) add(4 * q + k, weighted ? __fmul_rn(ldf(a, k), w) : ldf(a, k));
+        for (int t = 0; t < C / V; ++t) {
+            const float* p = row + 32 * V * t + V * lane;
+            if (V == 4) {
+                const float4 f = GLOBAL ? __ldg(reinterpret_cast<const float4*>(p))
+                                        : *reinterpret_cast<const float4*>(p);
+                x[4 * t] = f.x, x[4 * t + 1] = f.y, x[4 * t + 2] = f.z, x[4 * t + 3] = f.w;
+            } else if (V == 2) {
+                const float2 f = GLOBAL ? __ldg(reinterpret_cast<const float2*>(p))
+                                        : *reinterpret_cast<const float2*>(p);
+                x[2 * t] = f.x, x[2 * t + 1] = f.y;
+            } else {
+                x[t] = GLOBAL ? __ldg(p) : *p;
+            }
         }
     }
 };
 
-// Epilogue of row v for a lane's C columns (c0 = first column).
-template <int C>
-__device__ __forceinline__ void ppr_row(const PprArgs& A, uint32_t v, const float* sum,
-                                        uint32_t c0, float* dacc, float* sacc, const float* ps,
-                                        uint32_t frozen_bits) {
-    const double dg = A.deg[v];
-    const bool snk = A.sink[v];
-    const float fdeg = (float)dg;
-    const float inv = dg != 0.0 ? (float)(1.0 / dg) : 0.f;
-    const uint32_t sb = A.seed_off[v], se = A.seed_off[v + 1];
-    const float* zp = A.zprev + (size_t)v * A.Bp + c0;
-    float* zn = A.znext + (size_t)v * A.Bp + c0;
-#pragma unroll
-    for (int q = 0; q < C / 4; ++q) {
-        const float4 z4 = *reinterpret_cast<const float4*>(zp + 4 * q);
-        float o[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int c = 4 * q + k;
-            const float z = ldf(z4, k);
-            const float prev = snk ? z : __fmul_rn(z, fdeg);
-            float pv = 0.f;
-            for (uint32_t t = sb; t < se; ++t) {
-                const uint2 sd = A.seeds[t];
-                if (sd.x == c0 + c) pv = __uint_as_float(sd.y);
-            }
-            float nv;
-            if ((frozen_bits >> c) & 1u) {
-                nv = prev;
-            } else {
-                const float r = __fadd_rn(__fmul_rn(ps[c], pv), sum[c]);
-                nv = __fadd_rn(__fmul_rn(A.one_minus_d, pv), __fmul_rn(A.d, r));
-                dacc[c] = __fadd_rn(dacc[c], fabsf(__fsub_rn(nv, prev)));
-            }
-            if (snk) sacc[c] = __fadd_rn(sacc[c], nv);
-            o[k] = snk ? nv : __fmul_rn(nv, inv);
+// Sum of zin rows over the pull entries [pb, pe) for a lane's C slots: the
+// warp loads 32 entries at a time and keeps U gathered rows in flight.  The
+// U rows of a round are summed plainly and the round's sum is added with
+// compensation (blocked Kahan summation).
+template <int C, int U, bool W>
+__device__ __forceinline__ void gather(const PprArgs& A, uint32_t pb, uint32_t pe, int lane,
+                                       Acc<C>& acc) {
+    for (uint32_t p0 = pb; p0 < pe; p0 += 32) {
+        const uint32_t cnt = min(32u, pe - p0);
+        uint32_t my = 0;
+        float mw = 1.f;
+        if ((uint32_t)lane < cnt) {
+            my = __ldg(A.other + p0 + lane);
+            if (W) mw = __ldg(A.w + p0 + lane);
         }
-        *reinterpret_cast<float4*>(zn + 4 * q) = make_float4(o[0], o[1], o[2], o[3]);
+        for (uint32_t k = 0; k < cnt; k += U) {
+            float v[U][C];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t src = __shfl_sync(0xffffffffu, my, (k + u) & 31);
+                if (k + u < cnt) Lanes<C>::template load<true>(A.zin + (size_t)src * A.s_in, lane, v[u]);
+            }
+            float t[C];
+#pragma unroll
+            for (int q = 0; q < C; ++q) t[q] = 0.f;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const float ww = W ? __shfl_sync(0xffffffffu, mw, (k + u) & 31) : 1.f;
+                if (k + u < cnt) {
+#pragma unroll
+                    for (int q = 0; q < C; ++q)
+                        t[q] = __fadd_rn(t[q], W ? __fmul_rn(v[u][q], ww) : v[u][q]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < C; ++q) acc.add(q, t[q]);
+        }
     }
 }
 
-// One sweep over all B columns.  Phase 1: each long row by one CTA (warp w
-// sums in-edges w, w+8, ... in order; the warps' partials merge in warp
-// order).  Phase 2: a warp per remaining row, heaviest first.  Every
-// assignment is a fixed stride, so the sums do not depend on timing.
+// What the epilogue of row v reads besides the row sums, loaded before the
+// gathers so that its latency overlaps them.
 template <int C>
-__global__ void __launch_bounds__(PPR_NT) k_ppr_sweep(PprArgs A) {
-    extern __shared__ float2 lpart[];  // [PPR_WARPS][Bp] for phase 1
-    __shared__ double red[PPR_WARPS][128];
-    __shared__ bool last;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t c0 = lane * C;
-    const bool W = A.w != nullptr;
-    float ps[C], dacc[C], sacc[C];
-    uint32_t frozen_bits = 0;
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-        ps[c] = (float)A.psink[c0 + c];
-        dacc[c] = 0.f, sacc[c] = 0.f;
-        if (A.frozen[c0 + c]) frozen_bits |= 1u << c;
+struct RowIn {
+    float2 dd;
+    uint32_t sb, se;
+    float z[C];  // zin[v] of the lane's slots
+    __device__ __forceinline__ void load(const PprArgs& A, uint32_t v, int lane) {
+        dd = A.dinv[v];
+        sb = A.seed_off[v];
+        se = A.seed_off[v + 1];
+        Lanes<C>::template load<true>(A.zin + (size_t)v * A.s_in, lane, z);
     }
-    Acc<C> acc;
-    // ---- phase 1: long rows, a CTA each ----
-    for (uint32_t k = blockIdx.x; k < A.n_long; k += gridDim.x) {
-        const uint32_t v = A.longs[k];
-        const uint32_t b = A.off[v], e = A.off[v + 1];
-        acc.zero();
-        for (uint32_t p = b + warp; p < e; p += PPR_WARPS)
-            acc.add_row(A.zprev, A.Bp, __ldg(A.other + p), c0, W ? __ldg(A.w + p) : 1.f, W);
+};
+
+// Compensated FP32 accumulation into a shared-memory slot {s, c} (value s - c).
+__device__ __forceinline__ void smem_kahan_add(float2* acc, float x) {
+    float2 a = *acc;
+    const float y = __fsub_rn(x, a.y);
+    const float t = __fadd_rn(a.x, y);
+    a.y = __fsub_rn(__fsub_rn(t, a.x), y);
+    a.x = t;
+    *acc = a;
+}
+
+// Row v's new values for a lane's C input slots, written to zout in the
+// output layout through the warp's staging row (empty output slots stay 0);
+// the L1 change and dangling mass go to the warp's compensated accumulators,
+// held at position 32 q + lane for the lane's q-th slot (conflict-free).
+// Nothing here runs on the FP64 pipe.
+template <int C>
+__device__ __forceinline__ void finish_row(const PprArgs& A, uint32_t v, const RowIn<C>& r,
+                                           const float (&sum)[C], int lane, float2* dz,
+                                           float2* sk, float* stage) {
+    const bool snk = r.dd.x < 0.f;
 #pragma unroll
-        for (int c = 0; c < C; ++c) lpart[warp * A.Bp + c0 + c] = make_float2(acc.s[c], -acc.c[c]);
-        __syncthreads();
-        if (warp == 0) {
+    for (int q = 0; q < C; ++q) {
+        const uint32_t j = Lanes<C>::slot(lane, q);
+        const uint32_t os = __ldg(A.out_slot + j);
+        if (os == PPR_NONE) continue;
+        const uint32_t col = __ldg(A.col_in + j);
+        const float prev = snk ? r.z[q] : __fmul_rn(r.z[q], r.dd.x);
+        float pv = 0.f;
+        for (uint32_t t = r.sb; t < r.se; ++t) {
+            const uint2 sd = A.seeds[t];
+            if (sd.x == col) pv = __uint_as_float(sd.y);
+        }
+        const float x = __fadd_rn(__fmul_rn(__ldg(A.psink + j), pv), sum[q]);
+        const float nv = __fadd_rn(__fmul_rn(A.one_minus_d, pv), __fmul_rn(A.d, x));
+        smem_kahan_add(dz + 32 * q + lane, fabsf(__fsub_rn(nv, prev)));
+        if (snk) smem_kahan_add(sk + 32 * q + lane, nv);
+        stage[os] = snk ? nv : __fmul_rn(nv, r.dd.y);
+    }
+    __syncwarp();
+    float* zn = A.zout + (size_t)v * A.s_out + lane;
+    for (uint32_t j = 0; j < A.s_out; j += 32) zn[j] = stage[j + lane];
+    __syncwarp();
+}
+
+// Shared memory of both kernels: per warp [s_in] compensated change and mass
+// and a staging row of s_in floats.
+inline size_t ppr_smem(uint32_t s_in) {
+    return (size_t)PPR_WARPS * s_in * (2 * sizeof(float2) + sizeof(float));
+}
+
+struct WarpSmem {
+    float2 *dz_all, *sk_all, *dz, *sk;
+    float* stage;
+    __device__ __forceinline__ WarpSmem(float2* sm, uint32_t s_in, int warp, int lane) {
+        dz_all = sm;
+        sk_all = sm + PPR_WARPS * s_in;
+        dz = dz_all + warp * s_in;
+        sk = sk_all + warp * s_in;
+        stage = reinterpret_cast<float*>(sk_all + PPR_WARPS * s_in) + warp * s_in;
+        for (uint32_t j = lane; j < s_in; j += 32)
+            dz[j] = make_float2(0.f, 0.f), sk[j] = make_float2(0.f, 0.f), stage[j] = 0.f;
+        __syncwarp();
+    }
+};
+
+// The CTA's per-slot sums (warps in order, FP64) into its partial record.
+template <int C>
+__device__ __forceinline__ void cta_fold(const PprArgs& A, const WarpSmem& m) {
+    __syncthreads();
+    double* dst = A.part + (size_t)(A.part_base + blockIdx.x) * 2 * A.s_in;
+    for (uint32_t pos = threadIdx.x; pos < A.s_in; pos += PPR_NT) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < PPR_WARPS; ++w) {
+            const float2 x = m.dz_all[w * A.s_in + pos], y = m.sk_all[w * A.s_in + pos];
+            a += (double)x.x - (double)x.y;
+            b += (double)y.x - (double)y.y;
+        }
+        const uint32_t j = Lanes<C>::slot(pos & 31, pos >> 5);
+        dst[j] = a;
+        dst[A.s_in + j] = b;
+    }
+}
+
+// Sweep, part 1: every long-row chunk (partials to cpart) and every single
+// row (finished here).  Warp gw takes items gw, gw + warps, ... and loads
+// each next item while it works on the current one.
+template <int C, int U, bool W>
+__global__ void __launch_bounds__(PPR_NT) k_ppr_rows(PprArgs A) {
+    extern __shared__ float2 ppr_sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const WarpSmem m(ppr_sm, A.s_in, warp, lane);
+    const uint32_t gw = blockIdx.x * PPR_WARPS + warp, nw = gridDim.x * PPR_WARPS;
+    uint4 nxt = gw < A.n_items ? A.items[gw] : make_uint4(0u, 0u, 0u, 0u);
+    for (uint32_t it = gw; it < A.n_items; it += nw) {
+        const uint4 cur = nxt;
+        if (it + nw < A.n_items) nxt = A.items[it + nw];
+        Acc<C> acc;
+        acc.zero();
+        if (it < A.n_chunks) {
+            gather<C, U, W>(A, cur.y, cur.z, lane, acc);
+            float2* dst = A.cpart + (size_t)it * A.s_in;
+#pragma unroll
+            for (int q = 0; q < C; ++q)
+                __stcg(dst + Lanes<C>::slot(lane, q), make_float2(acc.s[q], -acc.c[q]));
+        } else {
+            RowIn<C> r;
+            r.load(A, cur.x, lane);
+            gather<C, U, W>(A, cur.y, cur.z, lane, acc);
             float sum[C];
 #pragma unroll
-            for (int c = 0; c < C; ++c) {
-                Kahan t;
-                for (int wv = 0; wv < PPR_WARPS; ++wv) {
-                    const float2 q = lpart[wv * A.Bp + c0 + c];
-                    t.merge(q.x, q.y);
-                }
-                sum[c] = t.value();
-            }
-            ppr_row<C>(A, v, sum, c0, dacc, sacc, ps, frozen_bits);
+            for (int q = 0; q < C; ++q) sum[q] = __fsub_rn(acc.s[q], acc.c[q]);
+            finish_row<C>(A, cur.x, r, sum, lane, m.dz, m.sk, m.stage);
         }
-        __syncthreads();
     }
-    // ---- phase 2: a warp per row ----
-    const uint32_t gw = blockIdx.x * PPR_WARPS + warp, nw = gridDim.x * PPR_WARPS;
-    for (uint32_t it = gw; it < A.n_rows; it += nw) {
-        const uint32_t v = A.rows[it];
-        const uint32_t b = A.off[v], e = A.off[v + 1];
-        acc.zero();
-        uint32_t p = b;
-        for (; p + 2 <= e; p += 2) {  // two gathered rows in flight
-            const uint32_t s0 = __ldg(A.other + p), s1 = __ldg(A.other + p + 1);
-            const float w0 = W ? __ldg(A.w + p) : 1.f, w1 = W ? __ldg(A.w + p + 1) : 1.f;
-            acc.add_row(A.zprev, A.Bp, s0, c0, w0, W);
-            acc.add_row(A.zprev, A.Bp, s1, c0, w1, W);
+    cta_fold<C>(A, m);
+}
+
+
+// --------------------------------------------------------------------------
+// Sweep, part 1, bulk-copy variant.  The gather of a row of zin (S floats,
+// 128-byte aligned) is one cp.async.bulk into shared memory, completed on an
+// mbarrier, so the rows in flight sit in shared memory instead of registers.
+// Each warp streams its items as batches of up to BT rows through a
+// two-batch ring: while batch k is summed, the copies of batch k+1 are in
+// flight and the source indices of batch k+2 are being loaded.
+// --------------------------------------------------------------------------
+
+constexpr int PB_WARPS = 4;
+constexpr int PB_NT = 32 * PB_WARPS;
+constexpr long long PB_WAIT_CYCLES = 4000000000ll;  // ~2 s: a copy that never lands
+constexpr uint32_t PB_BLOCK = 8;                    // rows per plain partial sum
+
+// rows per batch: about 4 KB of rows, 2..32
+constexpr int pb_rows(int C) { return 32 / C >= 2 ? (32 / C > 32 ? 32 : 32 / C) : 2; }
+
+template <int C>
+struct PbLayout {
+    static constexpr int S = 32 * C;
+    static constexpr int BT = pb_rows(C);
+    static constexpr int RING = 2 * BT * S * 4;               // bytes
+    static constexpr int DZ = RING + 16;                      // after the two mbarriers
+    static constexpr int SK = DZ + S * 8;
+    static constexpr int ST = SK + S * 8;
+    static constexpr int WARP = ((ST + S * 4) + 127) / 128 * 128;  // per-warp bytes
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\t"
+        "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(bar),
+        "r"(bytes)
+        : "memory");
+}
+
+// Bounded wait for the phase of the given parity; false if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > PB_WAIT_CYCLES) return false;
+    }
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+struct PbBatch {
+    uint32_t it, v, p, cnt;
+    bool first, last, valid;
+};
+
+template <int C, bool W>
+__global__ void __launch_bounds__(PB_NT) k_ppr_bulk(PprArgs A) {
+    using Lay = PbLayout<C>;
+    constexpr int S = Lay::S, BT = Lay::BT;
+    extern __shared__ __align__(128) unsigned char pb_sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned char* wsm = pb_sm + warp * Lay::WARP;
+    float* ring = reinterpret_cast<float*>(wsm);
+    const uint32_t bar0 = smem_u32(wsm + Lay::RING);
+    float2* dz = reinterpret_cast<float2*>(wsm + Lay::DZ);
+    float2* sk = reinterpret_cast<float2*>(wsm + Lay::SK);
+    float* stage = reinterpret_cast<float*>(wsm + Lay::ST);
+    for (int j = lane; j < S; j += 32)
+        dz[j] = make_float2(0.f, 0.f), sk[j] = make_float2(0.f, 0.f), stage[j] = 0.f;
+    if (lane == 0) {
+        mbar_init(bar0);
+        mbar_init(bar0 + 8);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+
+    const uint32_t gw = blockIdx.x * PB_WARPS + warp, nw = gridDim.x * PB_WARPS;
+    // the batch generator (warp-uniform state)
+    uint32_t g_it = gw;
+    uint4 g_rec = g_it < A.n_items ? A.items[g_it] : make_uint4(0u, 0u, 0u, 0u);
+    uint4 g_nxt = g_it + nw < A.n_items ? A.items[g_it + nw] : make_uint4(0u, 0u, 0u, 0u);
+    uint32_t g_p = g_rec.y;
+    auto next_batch = [&]() {
+        PbBatch b{};
+        if (g_it >= A.n_items) return b;
+        b.valid = true;
+        b.it = g_it;
+        b.v = g_rec.x;
+        b.p = g_p;
+        b.cnt = min((uint32_t)BT, g_rec.z - g_p);
+        b.first = g_p == g_rec.y;
+        b.last = g_p + b.cnt == g_rec.z;
+        g_p += b.cnt;
+        if (b.last) {
+            g_it += nw;
+            g_rec = g_nxt;
+            g_p = g_rec.y;
+            if (g_it + nw < A.n_items) g_nxt = A.items[g_it + nw];
         }
-        if (p < e) acc.add_row(A.zprev, A.Bp, __ldg(A.other + p), c0, W ? __ldg(A.w + p) : 1.f, W);
+        return b;
+    };
+
+    PbBatch bA = next_batch(), bB{}, bC{};
+    uint32_t iA = 0;
+    float wA = 1.f;
+    if (bA.valid && (uint32_t)lane < bA.cnt) {
+        iA = __ldg(A.other + bA.p + lane);
+        if (W) wA = __ldg(A.w + bA.p + lane);
+    }
+    float wB = 1.f, wC = 1.f;
+    RowIn<C> rB, rC;
+    uint32_t hB = 0, parity = 0;  // half of the batch being issued; phase bit per half
+    Acc<C> acc;
+    acc.zero();
+    bool ok = true;
+    for (;;) {
+        // stage 2: the copies of batch A into half hB
+        bB = bA;
+        wB = wA;
+        if (bB.valid && bB.cnt > 0) {
+            const uint32_t bar = bar0 + 8 * hB;
+            if (lane == 0) mbar_expect(bar, bB.cnt * (uint32_t)(S * 4));
+            __syncwarp();
+            if ((uint32_t)lane < bB.cnt)
+                bulk_g2s(smem_u32(ring + (size_t)(hB * BT + lane) * S), A.zin + (size_t)iA * S,
+                         S * 4, bar);
+        }
+        if (bB.valid && bB.first && bB.it >= A.n_chunks) rB.load(A, bB.v, lane);
+        // stage 1: the source indices of the batch after it
+        bA = next_batch();
+        if (bA.valid && (uint32_t)lane < bA.cnt) {
+            iA = __ldg(A.other + bA.p + lane);
+            if (W) wA = __ldg(A.w + bA.p + lane);
+        }
+        // stage 3: sum batch C (half hB ^ 1)
+        if (bC.valid) {
+            const uint32_t h = hB ^ 1u;
+            if (bC.cnt > 0) {
+                if (!mbar_wait(bar0 + 8 * h, (parity >> h) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                parity ^= 1u << h;
+            }
+            if (bC.first) acc.zero();
+            const float* rb = ring + (size_t)h * BT * S;
+            for (uint32_t i0 = 0; i0 < bC.cnt; i0 += PB_BLOCK) {
+                // blocked Kahan: up to PB_BLOCK rows summed plainly, then added
+                float t[C];
+#pragma unroll
+                for (int q = 0; q < C; ++q) t[q] = 0.f;
+                const uint32_t i1 = min(bC.cnt, i0 + PB_BLOCK);
+                for (uint32_t i = i0; i < i1; ++i) {
+                    const float ww = W ? __shfl_sync(0xffffffffu, wC, i) : 1.f;
+                    float x[C];
+                    Lanes<C>::template load<false>(rb + (size_t)i * S, lane, x);
+#pragma unroll
+                    for (int q = 0; q < C; ++q) t[q] = __fadd_rn(t[q], W ? __fmul_rn(x[q], ww) : x[q]);
+                }
+#pragma unroll
+                for (int q = 0; q < C; ++q) acc.add(q, t[q]);
+            }
+            if (bC.last) {
+                if (bC.it < A.n_chunks) {
+                    float2* dst = A.cpart + (size_t)bC.it * A.s_in;
+#pragma unroll
+                    for (int q = 0; q < C; ++q)
+                        __stcg(dst + Lanes<C>::slot(lane, q), make_float2(acc.s[q], -acc.c[q]));
+                } else {
+                    float sum[C];
+#pragma unroll
+                    for (int q = 0; q < C; ++q) sum[q] = __fsub_rn(acc.s[q], acc.c[q]);
+                    finish_row<C>(A, bC.v, rC, sum, lane, dz, sk, stage);
+                }
+            }
+            // the half is refilled by the async proxy next: order our reads first
+            __syncwarp();
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        // rotate
+        if (!bB.valid) break;
+        bC = bB;
+        wC = wB;
+        if (bB.first) rC = rB;
+        hB ^= 1u;
+    }
+    if (!ok) {
+        // give the copies still in flight a bounded chance to land and report;
+        // the host discards this sweep
+        if (lane == 0) atomicExch(A.err, 1);
+        if (bB.valid && bB.cnt > 0) (void)mbar_wait(bar0 + 8 * hB, (parity >> hB) & 1u);
+    }
+    // the CTA's per-slot sums (warps in order, FP64) into its partial record
+    __syncthreads();
+    double* dst = A.part + (size_t)(A.part_base + blockIdx.x) * 2 * A.s_in;
+    for (uint32_t pos = threadIdx.x; pos < (uint32_t)S; pos += PB_NT) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < PB_WARPS; ++w) {
+            const unsigned char* o = pb_sm + w * Lay::WARP;
+            const float2 x = reinterpret_cast<const float2*>(o + Lay::DZ)[pos];
+            const float2 y = reinterpret_cast<const float2*>(o + Lay::SK)[pos];
+            a += (double)x.x - (double)x.y;
+            b += (double)y.x - (double)y.y;
+        }
+        const uint32_t j = Lanes<C>::slot(pos & 31, pos >> 5);
+        dst[j] = a;
+        dst[A.s_in + j] = b;
+    }
+}
+
+// Sweep, part 2: every long row, its chunks' partials merged in chunk order.
+template <int C>
+__global__ void __launch_bounds__(PPR_NT) k_ppr_long(PprArgs A) {
+    extern __shared__ float2 ppr_sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const WarpSmem m(ppr_sm, A.s_in, warp, lane);
+    const uint32_t gw = blockIdx.x * PPR_WARPS + warp, nw = gridDim.x * PPR_WARPS;
+    for (uint32_t k = gw; k < A.n_long; k += nw) {
+        const uint4 lr = A.longs[k];
+        RowIn<C> r;
+        r.load(A, lr.x, lane);
+        Kahan t[C];
+        for (uint32_t c = lr.y; c < lr.y + lr.z; ++c) {
+            const float2* src = A.cpart + (size_t)c * A.s_in;
+#pragma unroll
+            for (int q = 0; q < C; ++q) {
+                const float2 pq = __ldcg(src + Lanes<C>::slot(lane, q));
+                t[q].merge(pq.x, pq.y);
+            }
+        }
         float sum[C];
 #pragma unroll
-        for (int c = 0; c < C; ++c) sum[c] = __fsub_rn(acc.s[c], acc.c[c]);
-        ppr_row<C>(A, v, sum, c0, dacc, sacc, ps, frozen_bits);
+        for (int q = 0; q < C; ++q) sum[q] = t[q].value();
+        finish_row<C>(A, lr.x, r, sum, lane, m.dz, m.sk, m.stage);
     }
-    // ---- per-column fold: warps -> CTA partial, CTAs -> last CTA (fixed order) ----
-    const uint32_t Bp = A.Bp;
-    for (uint32_t base = 0; base < Bp; base += 64) {
-#pragma unroll
-        for (int c = 0; c < C; ++c) {
-            const uint32_t bc = c0 + c;
-            if (bc >= base && bc < base + 64) {
-                red[warp][bc - base] = (double)dacc[c];
-                red[warp][64 + bc - base] = (double)sacc[c];
-            }
-        }
-        __syncthreads();
-        if (tid < 128) {
-            double t = 0.0;
-            for (int wv = 0; wv < PPR_WARPS; ++wv) t += red[wv][tid];
-            const uint32_t bc = base + (tid & 63);
-            A.part[(size_t)blockIdx.x * 2 * Bp + (tid < 64 ? bc : Bp + bc)] = t;
-        }
-        __syncthreads();
-    }
-    if (tid == 0) {
-        __threadfence();
-        last = atomicAdd(A.ticket, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last) {
-        __threadfence();
-        for (uint32_t bc = tid; bc < 2 * Bp; bc += PPR_NT) {
-            double t8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            unsigned k = 0;
-            for (; k + 8 <= gridDim.x; k += 8) {
-#pragma unroll
-                for (int j = 0; j < 8; ++j) t8[j] += __ldcg(A.part + (size_t)(k + j) * 2 * Bp + bc);
-            }
-            for (; k < gridDim.x; ++k) t8[0] += __ldcg(A.part + (size_t)k * 2 * Bp + bc);
-            double t = 0.0;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) t += t8[j];
-            A.out[bc] = t;
-        }
-        if (tid == 0) *A.ticket = 0u;
-    }
+    cta_fold<C>(A, m);
 }
 
-// Initial iterate: rank_b = pers_b (a fresh map), stored as Z; and the
-// per-column dangling mass of it (host-side sum over the seeds, as seeds
-// are few).
-__global__ void k_ppr_init(uint32_t n, uint32_t Bp, const double* __restrict__ deg,
-                           const uint32_t* __restrict__ seed_off, const uint2* __restrict__ seeds,
+// Sweep, part 3: out[j] = sum over the CTA partials of both kernels, in a
+// fixed order (a thread per value).
+__global__ void k_ppr_fold(uint32_t n_values, uint32_t n_parts, const double* __restrict__ part,
+                           double* __restrict__ out) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_values) return;
+    double t8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t k = 0;
+    for (; k + 8 <= n_parts; k += 8) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) t8[i] += part[(size_t)(k + i) * n_values + j];
+    }
+    for (; k < n_parts; ++k) t8[0] += part[(size_t)k * n_values + j];
+    double t = 0.0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) t += t8[i];
+    out[j] = t;
+}
+
+// The start: rank_b = pers_b, stored as Z (slot = column) over a zeroed Z;
+// each (vertex, column) seed appears once.
+__global__ void k_ppr_init(uint32_t ns, uint32_t S, const uint32_t* __restrict__ sv,
+                           const uint2* __restrict__ sd, const float2* __restrict__ dinv,
                            float* __restrict__ z) {
-    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (size_t)n * Bp) return;
-    const uint32_t v = (uint32_t)(t / Bp), b = (uint32_t)(t % Bp);
-    float pv = 0.f;
-    for (uint32_t k = seed_off[v]; k < seed_off[v + 1]; ++k)
-        if (seeds[k].x == b) pv = __uint_as_float(seeds[k].y);
-    const double dg = deg[v];
-    z[t] = dg != 0.0 ? __fmul_rn(pv, (float)(1.0 / dg)) : pv;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ns) return;
+    const uint32_t v = sv[k];
+    const float pv = __uint_as_float(sd[k].y);
+    const float2 dd = dinv[v];
+    z[(size_t)v * S + sd[k].x] = dd.x < 0.f ? pv : __fmul_rn(pv, dd.y);
 }
 
-// out[b][v] = rank_b of original vertex v (transpose through shared memory)
-__global__ void k_ppr_store(uint32_t n, uint32_t B, uint32_t Bp, const uint32_t* __restrict__ perm,
-                            const double* __restrict__ deg, const uint8_t* __restrict__ sink,
+// {FP32 degree, its inverse} per vertex; {-1, 0} marks a sink.
+__global__ void k_ppr_dinv(uint32_t n, const double* __restrict__ deg, float2* __restrict__ dinv) {
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const double dg = deg[v];
+    dinv[v] = dg == 0.0 ? make_float2(-1.f, 0.f) : make_float2((float)dg, (float)(1.0 / dg));
+}
+
+// seed_off[v] = first seed record of vertex v (records sorted by vertex).
+__global__ void k_ppr_seed_off(uint32_t n, uint32_t ns, const uint32_t* __restrict__ sv,
+                               uint32_t* __restrict__ seed_off) {
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v > n) return;
+    uint32_t lo = 0, hi = ns;
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (sv[mid] < v)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    seed_off[v] = lo;
+}
+
+// Internal label and degree of each seed vertex.
+__global__ void k_ppr_seed_lookup(uint32_t ns, const uint32_t* __restrict__ orig,
+                                  const uint32_t* __restrict__ iperm, const double* __restrict__ deg,
+                                  uint32_t* __restrict__ iv, double* __restrict__ dv) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ns) return;
+    const uint32_t v = iperm[orig[k]];
+    iv[k] = v;
+    dv[k] = deg[v];
+}
+
+// out[col][perm i] = rank of column col at internal vertex i, for K
+// (slot, column) pairs (transposed through shared memory).
+__global__ void k_ppr_store(uint32_t n, uint32_t S, uint32_t K, const uint2* __restrict__ pairs,
+                            const uint32_t* __restrict__ perm, const float2* __restrict__ dinv,
                             const float* __restrict__ z, void* __restrict__ out, int dt) {
     __shared__ float tile[32][33];
-    const uint32_t i0 = blockIdx.x * 32, b0 = blockIdx.y * 32;
+    const uint32_t i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
     const uint32_t tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
     for (uint32_t r = ty; r < 32; r += 8) {
-        const uint32_t i = i0 + r, b = b0 + tx;
+        const uint32_t i = i0 + r, k = k0 + tx;
         float val = 0.f;
-        if (i < n && b < Bp) {
-            const float zz = z[(size_t)i * Bp + b];
-            val = sink[i] ? zz : __fmul_rn(zz, (float)deg[i]);
+        if (i < n && k < K) {
+            const float zz = z[(size_t)i * S + pairs[k].x];
+            const float2 dd = dinv[i];
+            val = dd.x < 0.f ? zz : __fmul_rn(zz, dd.x);
         }
         tile[r][tx] = val;
     }
     __syncthreads();
     for (uint32_t r = ty; r < 32; r += 8) {
-        const uint32_t b = b0 + r, i = i0 + tx;
-        if (b < B && i < n) {
-            const size_t o = (size_t)b * n + perm[i];
+        const uint32_t k = k0 + r, i = i0 + tx;
+        if (k < K && i < n) {
+            const size_t o = (size_t)pairs[k].y * n + perm[i];
             if (dt == GTC_F64)
                 ((double*)out)[o] = (double)tile[tx][r];
             else
@@ -283,35 +652,106 @@ __global__ void k_ppr_store(uint32_t n, uint32_t B, uint32_t Bp, const uint32_t*
     }
 }
 
-struct PprSchedule {
-    DevBuf<uint32_t> rows, longs;
-    uint32_t n_rows = 0, n_long = 0;
-};
+__global__ void k_degree_ppr(uint32_t n, const uint32_t* __restrict__ push_off,
+                             const uint32_t* __restrict__ push_eid, const void* __restrict__ w,
+                             int wdt, double* __restrict__ deg) {
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const uint32_t b = push_off[v], e = push_off[v + 1];
+    double k;
+    if (!w) {
+        k = (double)(e - b);
+    } else {
+        k = 0.0;
+        for (uint32_t p = b; p < e; ++p) k = __dadd_rn(k, ld_any(w, wdt, push_eid[p]));
+    }
+    deg[v] = k;
+}
 
-// Rows of the pull half: the longest go to CTAs, the rest to warps, heaviest
-// first (a stable order, so the schedule is a function of the graph).
-void build_ppr_schedule(const uint32_t* d_off, uint32_t n, cudaStream_t s, PprSchedule& S) {
-    std::vector<uint32_t> off((size_t)n + 1);
-    GTC_CUDA(cudaMemcpyAsync(off.data(), d_off, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost, s));
+__global__ void k_gather_w_ppr(uint32_t m, const uint32_t* __restrict__ eid,
+                               const void* __restrict__ w, int wdt, float* __restrict__ out) {
+    size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < m) out[p] = (float)ld_any(w, wdt, eid[p]);
+}
+
+// schedule keys: 0 for a row cut into chunks, else PPR_CHUNK + 1 - in-degree
+__global__ void k_ppr_keys(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ key,
+                           unsigned* __restrict__ n_long) {
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const uint32_t dg = off[v + 1] - off[v];
+    key[v] = dg > PPR_CHUNK ? 0u : PPR_CHUNK + 1 - dg;
+    if (dg > PPR_CHUNK) atomicAdd(n_long, 1u);
+}
+
+__global__ void k_ppr_row_items(uint32_t k, const uint32_t* __restrict__ pos,
+                                const uint32_t* __restrict__ off, uint32_t flag,
+                                uint4* __restrict__ rec) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    const uint32_t v = pos[i];
+    rec[i] = make_uint4(v, off[v], off[v + 1], flag);
+}
+
+// The schedule of one unfiltered view, built on the graph's home stream and
+// kept with the graph.
+void build_ppr_schedule(gtc_graph* g, const View& view, cudaStream_t s, PprSched& S) {
+    const uint32_t n = view.n;
+    cudaStream_t h = g->home;
     GTC_CUDA(cudaStreamSynchronize(s));
-    std::vector<uint32_t> rows, longs;
-    rows.reserve(n);
-    for (uint32_t v = 0; v < n; ++v) (off[v + 1] - off[v] > PPR_LONG ? longs : rows).push_back(v);
-    std::stable_sort(rows.begin(), rows.end(), [&](uint32_t a, uint32_t b) {
-        return off[a + 1] - off[a] > off[b + 1] - off[b];
-    });
-    std::stable_sort(longs.begin(), longs.end(), [&](uint32_t a, uint32_t b) {
-        return off[a + 1] - off[a] > off[b + 1] - off[b];
-    });
-    S.n_rows = (uint32_t)rows.size();
-    S.n_long = (uint32_t)longs.size();
-    S.rows.alloc(rows.size(), s);
-    S.longs.alloc(longs.size(), s);
-    if (!rows.empty())
-        GTC_CUDA(cudaMemcpyAsync(S.rows.get(), rows.data(), rows.size() * 4, cudaMemcpyHostToDevice, s));
-    if (!longs.empty())
-        GTC_CUDA(cudaMemcpyAsync(S.longs.get(), longs.data(), longs.size() * 4, cudaMemcpyHostToDevice, s));
-    GTC_CUDA(cudaStreamSynchronize(s));
+    uint64_t L = 0;
+    DevBuf<uint32_t> key(n, h), skey(n, h), pos(n, h);
+    DevBuf<unsigned> cnt(1, h);
+    GTC_CUDA(cudaMemsetAsync(cnt.get(), 0, sizeof(unsigned), h));
+    if (n) {
+        k_ppr_keys<<<grid_for(n, 256, 1u << 30), 256, 0, h>>>(n, view.pull_off, key.get(), cnt.get());
+        GTC_LAUNCHED();
+        L++;
+        sort_positions_by_key(key.get(), n, PPR_CHUNK + 2, skey.get(), pos.get(), h, &L);
+    }
+    unsigned n_long = 0;
+    GTC_CUDA(cudaMemcpyAsync(&n_long, cnt.get(), sizeof(unsigned), cudaMemcpyDeviceToHost, h));
+    GTC_CUDA(cudaStreamSynchronize(h));
+    std::vector<uint4> lrec(n_long);
+    if (n_long) {
+        DevBuf<uint4> drec(n_long, h);
+        k_ppr_row_items<<<grid_for(n_long, 256, 1u << 30), 256, 0, h>>>(
+            n_long, pos.get(), view.pull_off, 0u, drec.get());
+        GTC_LAUNCHED();
+        L++;
+        GTC_CUDA(cudaMemcpyAsync(lrec.data(), drec.get(), n_long * sizeof(uint4),
+                                 cudaMemcpyDeviceToHost, h));
+        GTC_CUDA(cudaStreamSynchronize(h));
+    }
+    std::vector<uint4> chunks, longs(n_long);
+    for (uint32_t j = 0; j < n_long; ++j) {
+        const uint4 r = lrec[j];
+        const uint32_t first = (uint32_t)chunks.size();
+        for (uint32_t b = r.y; b < r.z; b += PPR_CHUNK)
+            chunks.push_back(make_uint4(r.x, b, std::min(r.z, b + PPR_CHUNK), j));
+        longs[j] = make_uint4(r.x, first, (uint32_t)chunks.size() - first, 0u);
+    }
+    const uint32_t n_single = n - n_long;
+    S.n_long = n_long;
+    S.n_chunks = (uint32_t)chunks.size();
+    S.n_items = S.n_chunks + n_single;
+    S.items.alloc(S.n_items, h);
+    S.longs.alloc(S.n_long, h);
+    if (S.n_chunks)
+        GTC_CUDA(cudaMemcpyAsync(S.items.get(), chunks.data(), chunks.size() * sizeof(uint4),
+                                 cudaMemcpyHostToDevice, h));
+    if (n_single) {
+        k_ppr_row_items<<<grid_for(n_single, 256, 1u << 30), 256, 0, h>>>(
+            n_single, pos.get() + n_long, view.pull_off, PPR_NONE, S.items.get() + S.n_chunks);
+        GTC_LAUNCHED();
+        L++;
+    }
+    if (S.n_long)
+        GTC_CUDA(cudaMemcpyAsync(S.longs.get(), longs.data(), longs.size() * sizeof(uint4),
+                                 cudaMemcpyHostToDevice, h));
+    GTC_CUDA(cudaStreamSynchronize(h));
+    S.built = true;
+    g->launches += L;
 }
 
 inline uint32_t host_float_bits(float f) {
@@ -319,20 +759,15 @@ inline uint32_t host_float_bits(float f) {
     std::memcpy(&u, &f, 4);
     return u;
 }
-inline float host_bits_float(uint32_t u) {
-    float f;
-    std::memcpy(&f, &u, 4);
-    return f;
-}
 
-struct Timer_ {
+struct PprTimer {
     cudaEvent_t a = nullptr, b = nullptr;
     cudaStream_t s;
-    explicit Timer_(cudaStream_t st) : s(st) {
+    explicit PprTimer(cudaStream_t st) : s(st) {
         GTC_CUDA(cudaEventCreate(&a));
         GTC_CUDA(cudaEventCreate(&b));
     }
-    ~Timer_() {
+    ~PprTimer() {
         if (a) cudaEventDestroy(a);
         if (b) cudaEventDestroy(b);
     }
@@ -346,45 +781,107 @@ struct Timer_ {
     }
 };
 
+// gathered rows in flight per warp: about 32 loads per lane
+constexpr int ppr_unroll(int C) { return C <= 1 ? 16 : C <= 4 ? 8 : C <= 8 ? 4 : 2; }
+
+// The two gather variants of part 1: loads into registers, or bulk copies
+// into shared memory.
+enum PprVariant { PPR_REGS = 0, PPR_BULK = 1 };
+
+struct PprLaunch {
+    unsigned grid1, threads1;
+    size_t smem1;
+};
+
+// Part 1's launch shape: as many CTAs as fit on every SM at once.
 template <int C>
-void launch_ppr(const PprArgs& A, unsigned grid, cudaStream_t s) {
-    const size_t dyn = (size_t)PPR_WARPS * A.Bp * sizeof(float2);
-    k_ppr_sweep<C><<<grid, PPR_NT, dyn, s>>>(A);
+PprLaunch ppr_shape(int variant, bool weighted) {
+    int per_sm = 0, sms = 0, dev = 0;
+    GTC_CUDA(cudaGetDevice(&dev));
+    GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const size_t smem_long = ppr_smem(32 * C);
+    GTC_CUDA(cudaFuncSetAttribute(k_ppr_long<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem_long));
+    PprLaunch L{};
+    if (variant == PPR_BULK) {
+        auto* f = weighted ? k_ppr_bulk<C, true> : k_ppr_bulk<C, false>;
+        L.threads1 = PB_NT;
+        L.smem1 = (size_t)PB_WARPS * PbLayout<C>::WARP;
+        GTC_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem1));
+        GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, PB_NT, L.smem1));
+    } else {
+        auto* f = weighted ? k_ppr_rows<C, ppr_unroll(C), true> : k_ppr_rows<C, ppr_unroll(C), false>;
+        L.threads1 = PPR_NT;
+        L.smem1 = smem_long;
+        GTC_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem1));
+        GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, PPR_NT, L.smem1));
+    }
+    L.grid1 = (unsigned)std::max(1, per_sm * sms);
+    return L;
+}
+
+template <int C>
+void launch_ppr(PprArgs A, int variant, const PprLaunch& L1, unsigned grid2, cudaStream_t s) {
+    A.part_base = 0;
+    if (variant == PPR_BULK) {
+        if (A.w)
+            k_ppr_bulk<C, true><<<L1.grid1, PB_NT, L1.smem1, s>>>(A);
+        else
+            k_ppr_bulk<C, false><<<L1.grid1, PB_NT, L1.smem1, s>>>(A);
+    } else {
+        if (A.w)
+            k_ppr_rows<C, ppr_unroll(C), true><<<L1.grid1, PPR_NT, L1.smem1, s>>>(A);
+        else
+            k_ppr_rows<C, ppr_unroll(C), false><<<L1.grid1, PPR_NT, L1.smem1, s>>>(A);
+    }
+    GTC_LAUNCHED();
+    A.part_base = L1.grid1;
+    k_ppr_long<C><<<grid2, PPR_NT, ppr_smem(32 * C), s>>>(A);
     GTC_LAUNCHED();
 }
 
-template <int C>
-unsigned ppr_grid(uint32_t Bp) {
-    int per_sm = 0, sms = 0, dev = 0;
-    const int dyn = PPR_WARPS * (int)Bp * (int)sizeof(float2);
-    GTC_CUDA(cudaGetDevice(&dev));
-    GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    GTC_CUDA(cudaFuncSetAttribute(k_ppr_sweep<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-    GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ppr_sweep<C>, PPR_NT, dyn));
-    return (unsigned)std::max(1, per_sm * sms);
+void fold(const PprArgs& A, unsigned n_parts, double* out, cudaStream_t s) {
+    const uint32_t nv = 2 * A.s_in;
+    k_ppr_fold<<<(nv + 63) / 64, 64, 0, s>>>(nv, n_parts, A.part, out);
+    GTC_LAUNCHED();
 }
 
-__global__ void k_degree_ppr(uint32_t n, const uint32_t* __restrict__ push_off,
-                             const uint32_t* __restrict__ push_eid, const void* __restrict__ w,
-                             int wdt, double* __restrict__ deg, uint8_t* __restrict__ sink) {
-    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n) return;
-    const uint32_t b = push_off[v], e = push_off[v + 1];
-    double k;
-    if (!w) {
-        k = (double)(e - b);
-    } else {
-        k = 0.0;
-        for (uint32_t p = b; p < e; ++p) k = __dadd_rn(k, ld_any(w, wdt, push_eid[p]));
+// line counts a sweep runs at: 1-4, then multiples of 4 (vector loads)
+#define GTC_PPR_C(X) X(1) X(2) X(3) X(4) X(8) X(12) X(16)
+
+PprLaunch shape(uint32_t C, int variant, bool weighted) {
+    switch (C) {
+#define GTC_CASE(c) \
+    case c: return ppr_shape<c>(variant, weighted);
+        GTC_PPR_C(GTC_CASE)
+#undef GTC_CASE
     }
-    deg[v] = k;
-    sink[v] = k == 0.0 ? 1 : 0;
+    throw Error{GTC_ERR_CUDA, "batched personalised PageRank: bad slot count"};
 }
 
-__global__ void k_gather_w_ppr(uint32_t m, const uint32_t* __restrict__ eid,
-                               const void* __restrict__ w, int wdt, float* __restrict__ out) {
-    size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < m) out[p] = (float)ld_any(w, wdt, eid[p]);
+void run_sweep(uint32_t C, const PprArgs& A, int variant, const PprLaunch& L1, unsigned grid2,
+               cudaStream_t s) {
+    switch (C) {
+#define GTC_CASE(c) \
+    case c: launch_ppr<c>(A, variant, L1, grid2, s); return;
+        GTC_PPR_C(GTC_CASE)
+#undef GTC_CASE
+    }
+    throw Error{GTC_ERR_CUDA, "batched personalised PageRank: bad slot count"};
+}
+
+// Lines per row for `active` columns: ceil(active / 32), rounded up to a
+// multiple of 4 above 4 lines.
+inline uint32_t ppr_lines(uint32_t active) {
+    const uint32_t c = (active + 31) / 32;
+    return c <= 4 ? c : (c + 3) / 4 * 4;
+}
+
+// GTC_PPR_VARIANT=regs|bulk pins the gather variant (default bulk).
+int ppr_variant() {
+    const char* e = std::getenv("GTC_PPR_VARIANT");
+    if (e && std::strcmp(e, "regs") == 0) return PPR_REGS;
+    return PPR_BULK;
 }
 
 }  // namespace
@@ -401,46 +898,21 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     View view;
     view.prepare(g, vw, s, &L);
     const uint32_t n = view.n, B = in.B;
-    const uint32_t Bp = (B + 127) / 128 * 128;  // 128, 256, 384 or 512 columns
     const double d = in.damping;
-    // the seeds, by internal vertex label
-    std::vector<uint32_t> perm(n);
-    if (n) GTC_CUDA(cudaMemcpyAsync(perm.data(), g->perm.get(), (size_t)n * 4, cudaMemcpyDeviceToHost, s));
-    GTC_CUDA(cudaStreamSynchronize(s));
-    std::vector<uint32_t> iperm(n);
-    for (uint32_t i = 0; i < n; ++i) iperm[perm[i]] = i;
-    std::vector<uint32_t> cnt((size_t)n + 1, 0);
-    const uint64_t ns = in.seed_off[B];
-    for (uint64_t k = 0; k < ns; ++k) {
+    for (uint32_t b = 0; b < B; ++b)
+        GTC_REQUIRE(in.seed_off[b + 1] >= in.seed_off[b], GTC_ERR_ARG,
+                    "seed offsets must not decrease");
+    const uint64_t ns_all = in.seed_off[B];
+    GTC_REQUIRE(ns_all < (1ull << 31), GTC_ERR_ARG, "too many seeds");
+    for (uint64_t k = 0; k < ns_all; ++k)
         GTC_REQUIRE(in.seed_vertices[k] < n, GTC_ERR_INDEX, "a seed vertex is outside the vertex bound");
-        cnt[iperm[in.seed_vertices[k]] + 1]++;
-    }
-    for (uint32_t v = 0; v < n; ++v) cnt[v + 1] += cnt[v];
-    std::vector<uint2> seeds(ns ? ns : 1);
-    {
-        std::vector<uint32_t> fill(cnt.begin(), cnt.end() - 1);
-        for (uint32_t b = 0; b < B; ++b) {
-            const uint64_t sb = in.seed_off[b], se = in.seed_off[b + 1];
-            GTC_REQUIRE(se >= sb, GTC_ERR_ARG, "seed offsets must not decrease");
-            for (uint64_t k = sb; k < se; ++k) {
-                const double val = in.seed_values ? in.seed_values[k] : 1.0 / (double)(se - sb);
-                const float fv = (float)val;
-                seeds[fill[iperm[in.seed_vertices[k]]]++] = make_uint2(b, host_float_bits(fv));
-            }
-        }
-    }
-    DevBuf<uint32_t> dso((size_t)n + 1, s);
-    DevBuf<uint2> dseeds(seeds.size(), s);
-    GTC_CUDA(cudaMemcpyAsync(dso.get(), cnt.data(), ((size_t)n + 1) * 4, cudaMemcpyHostToDevice, s));
-    GTC_CUDA(cudaMemcpyAsync(dseeds.get(), seeds.data(), seeds.size() * sizeof(uint2),
-                             cudaMemcpyHostToDevice, s));
-    // degrees and sinks of the view
+    const uint32_t ns = (uint32_t)ns_all;
+
+    // degrees of the view and pull-ordered weights
     DevBuf<double> deg(n, s);
-    DevBuf<uint8_t> sink(n, s);
     if (n) {
         k_degree_ppr<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, view.push_off, view.push_eid,
-                                                              in.weight.p, in.weight.dtype,
-                                                              deg.get(), sink.get());
+                                                              in.weight.p, in.weight.dtype, deg.get());
         GTC_LAUNCHED();
         L++;
     }
@@ -452,105 +924,202 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
         GTC_LAUNCHED();
         L++;
     }
-    PprSchedule sched;
-    PprSchedule* S = &sched;
-    build_ppr_schedule(view.pull_off, n, s, sched);
-    // iterates and per-column state
-    const size_t zn = (size_t)n * Bp;
-    DevBuf<float> z0(zn, s), z1(zn, s);
-    DevBuf<unsigned> ticket(1, s);
-    GTC_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), s));
-    if (zn) {
-        k_ppr_init<<<grid_for(zn, TB, 1u << 30), TB, 0, s>>>(n, Bp, deg.get(), dso.get(),
-                                                             dseeds.get(), z0.get());
+    DevBuf<float2> dinv(n, s);
+    if (n) {
+        k_ppr_dinv<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, deg.get(), dinv.get());
         GTC_LAUNCHED();
         L++;
     }
-    // dangling mass of the start (the seeds on sinks), on the host
-    std::vector<uint8_t> hsink(n);
-    if (n) GTC_CUDA(cudaMemcpyAsync(hsink.data(), sink.get(), n, cudaMemcpyDeviceToHost, s));
-    GTC_CUDA(cudaStreamSynchronize(s));
-    std::vector<double> hps(Bp, 0.0);
-    for (uint32_t v = 0; v < n; ++v)
-        if (hsink[v])
-            for (uint32_t k = cnt[v]; k < cnt[v + 1]; ++k)
-                hps[seeds[k].x] += (double)host_bits_float(seeds[k].y);
-    DevBuf<double> out(2 * (size_t)Bp, s), psink(Bp, s);
-    GTC_CUDA(cudaMemcpyAsync(psink.get(), hps.data(), Bp * sizeof(double), cudaMemcpyHostToDevice, s));
-    std::vector<uint8_t> frozen(Bp, 0);
-    for (uint32_t b = B; b < Bp; ++b) frozen[b] = 1;  // padding columns never run
-    DevBuf<uint8_t> dfrozen(Bp, s);
-    const unsigned cap = Bp == 128 ? ppr_grid<4>(Bp) : Bp == 256 ? ppr_grid<8>(Bp)
-                       : Bp == 384 ? ppr_grid<12>(Bp) : ppr_grid<16>(Bp);
-    const unsigned grid = std::max(1u, std::min(cap, (S->n_rows + PPR_WARPS - 1) / PPR_WARPS +
-                                                         S->n_long));
-    DevBuf<double> part((size_t)grid * 2 * Bp, s);
+    PprSched& S = g->ppr_sched[view.reversed ? 1 : 0];
+    if (!S.built) build_ppr_schedule(g, view, s, S);
+
+    // the seeds: internal labels, one record per (vertex, column) -- the
+    // last value given for a pair wins -- sorted by vertex
+    std::vector<uint32_t> iv(ns);
+    std::vector<double> dv(ns);
+    if (ns) {
+        DevBuf<uint32_t> dorig(ns, s), div(ns, s);
+        DevBuf<double> ddv(ns, s);
+        GTC_CUDA(cudaMemcpyAsync(dorig.get(), in.seed_vertices, (size_t)ns * 4, cudaMemcpyHostToDevice, s));
+        k_ppr_seed_lookup<<<grid_for(ns, TB, 1u << 30), TB, 0, s>>>(ns, dorig.get(), g->iperm.get(),
+                                                                    deg.get(), div.get(), ddv.get());
+        GTC_LAUNCHED();
+        L++;
+        GTC_CUDA(cudaMemcpyAsync(iv.data(), div.get(), (size_t)ns * 4, cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaMemcpyAsync(dv.data(), ddv.get(), (size_t)ns * 8, cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+    }
+    struct Rec {
+        uint32_t v, col;
+        float val;
+        double deg;
+    };
+    std::vector<Rec> recs;
+    recs.reserve(ns);
+    for (uint32_t b = 0; b < B; ++b) {
+        const uint64_t sb = in.seed_off[b], se = in.seed_off[b + 1];
+        for (uint64_t k = sb; k < se; ++k) {
+            const double val = in.seed_values ? in.seed_values[k] : 1.0 / (double)(se - sb);
+            recs.push_back({iv[k], b, (float)val, dv[k]});
+        }
+    }
+    std::stable_sort(recs.begin(), recs.end(), [](const Rec& a, const Rec& b) {
+        return a.v != b.v ? a.v < b.v : a.col < b.col;
+    });
+    std::vector<Rec> uniq;
+    for (const Rec& r : recs) {
+        if (!uniq.empty() && uniq.back().v == r.v && uniq.back().col == r.col)
+            uniq.back() = r;
+        else
+            uniq.push_back(r);
+    }
+    const uint32_t nu = (uint32_t)uniq.size();
+    std::vector<uint32_t> hsv(nu ? nu : 1);
+    std::vector<uint2> hsd(nu ? nu : 1);
+    std::vector<double> psink_col(B, 0.0);  // dangling mass of each column's iterate
+    for (uint32_t k = 0; k < nu; ++k) {
+        hsv[k] = uniq[k].v;
+        hsd[k] = make_uint2(uniq[k].col, host_float_bits(uniq[k].val));
+        if (uniq[k].deg == 0.0) psink_col[uniq[k].col] += (double)uniq[k].val;
+    }
+    DevBuf<uint32_t> dsv(hsv.size(), s), dso((size_t)n + 1, s);
+    DevBuf<uint2> dsd(hsd.size(), s);
+    GTC_CUDA(cudaMemcpyAsync(dsv.get(), hsv.data(), hsv.size() * 4, cudaMemcpyHostToDevice, s));
+    GTC_CUDA(cudaMemcpyAsync(dsd.get(), hsd.data(), hsd.size() * sizeof(uint2), cudaMemcpyHostToDevice, s));
+    k_ppr_seed_off<<<grid_for((size_t)n + 1, TB, 1u << 30), TB, 0, s>>>(n, nu, dsv.get(), dso.get());
+    GTC_LAUNCHED();
+    L++;
+
+    // iterates: the first layout is slot = column
+    uint32_t C = ppr_lines(B);
+    uint32_t s_in = 32 * C;
+    const size_t zn = (size_t)n * s_in;
+    DevBuf<float> z0(zn, s), z1(zn, s);
+    if (zn) GTC_CUDA(cudaMemsetAsync(z0.get(), 0, zn * sizeof(float), s));
+    if (nu && n) {
+        k_ppr_init<<<grid_for(nu, TB, 1u << 30), TB, 0, s>>>(nu, s_in, dsv.get(), dsd.get(),
+                                                             dinv.get(), z0.get());
+        GTC_LAUNCHED();
+        L++;
+    }
+    int sms = 0, dev = 0;
+    GTC_CUDA(cudaGetDevice(&dev));
+    GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const unsigned grid1_max = (unsigned)sms * (2048 / 32);  // at most one CTA per warp slot
+    const unsigned grid2 =
+        std::max(1u, std::min((S.n_long + PPR_WARPS - 1) / PPR_WARPS, (unsigned)sms));
+    DevBuf<float2> cpart((size_t)S.n_chunks * s_in, s);
+    DevBuf<double> part((size_t)(grid1_max + grid2) * 2 * s_in, s), out(2 * (size_t)s_in, s);
+    DevBuf<uint32_t> dmap(2 * (size_t)s_in, s);  // col_in, then out_slot
+    DevBuf<float> dps(s_in, s);
+    DevBuf<uint2> dpairs(s_in, s);
+    DevBuf<int> derr(1, s);
+    GTC_CUDA(cudaMemsetAsync(derr.get(), 0, sizeof(int), s));
+    const int variant = ppr_variant();
 
     PprArgs A{};
-    A.n = n, A.Bp = Bp;
-    A.rows = S->rows.get(), A.n_rows = S->n_rows;
-    A.longs = S->longs.get(), A.n_long = S->n_long;
-    A.off = view.pull_off, A.other = view.pull_other, A.w = wpull.get();
-    A.deg = deg.get(), A.sink = sink.get();
-    A.seed_off = dso.get(), A.seeds = dseeds.get();
-    A.frozen = dfrozen.get();
-    A.psink = psink.get();
+    A.n = n;
+    A.items = S.items.get(), A.n_items = S.n_items, A.n_chunks = S.n_chunks;
+    A.longs = S.longs.get(), A.n_long = S.n_long;
+    A.other = view.pull_other, A.w = wpull.get();
+    A.dinv = dinv.get();
+    A.seed_off = dso.get(), A.seeds = dsd.get();
+    A.psink = dps.get();
     A.one_minus_d = (float)(1.0 - d), A.d = (float)d;
-    A.part = part.get(), A.ticket = ticket.get(), A.out = out.get();
+    A.cpart = cpart.get(), A.part = part.get(), A.err = derr.get();
 
-    std::vector<double> hout(2 * (size_t)Bp);
+    std::vector<uint32_t> col_in(s_in, PPR_NONE), out_slot, col_out, maps;
+    for (uint32_t b = 0; b < B; ++b) col_in[b] = b;
+    std::vector<uint8_t> done(B, 0);
+    std::vector<double> hout;
+    std::vector<float> hps;
+    std::vector<uint2> store;
     std::fill(in.iters, in.iters + B, 0);
     uint32_t running = B;
-    uint64_t sweep = 0;
+    uint64_t sweeps = 0;
+    double sweep_ms = 0.0;
     float *zc = z0.get(), *zx = z1.get();
-    Timer_ total(s);
+    PprTimer total(s), tsw(s);
     total.start();
     while (running > 0) {
-        GTC_CUDA(cudaMemcpyAsync(dfrozen.get(), frozen.data(), Bp, cudaMemcpyHostToDevice, s));
-        A.zprev = zc, A.znext = zx;
-        if (Bp == 128)
-            launch_ppr<4>(A, grid, s);
-        else if (Bp == 256)
-            launch_ppr<8>(A, grid, s);
-        else if (Bp == 384)
-            launch_ppr<12>(A, grid, s);
-        else
-            launch_ppr<16>(A, grid, s);
-        L++;
-        SL++;
-        GTC_CUDA(cudaMemcpyAsync(hout.data(), out.get(), 2 * Bp * sizeof(double),
+        // the output layout: the columns still running, packed
+        out_slot.assign(s_in, PPR_NONE);
+        col_out.clear();
+        for (uint32_t j = 0; j < s_in; ++j) {
+            const uint32_t c = col_in[j];
+            if (c == PPR_NONE || done[c]) continue;
+            out_slot[j] = (uint32_t)col_out.size();
+            col_out.push_back(c);
+        }
+        const uint32_t c_out = ppr_lines((uint32_t)col_out.size());
+        const uint32_t s_out = 32 * c_out;
+        col_out.resize(s_out, PPR_NONE);
+        hps.assign(s_in, 0.f);
+        for (uint32_t j = 0; j < s_in; ++j)
+            if (col_in[j] != PPR_NONE) hps[j] = (float)psink_col[col_in[j]];
+        maps.assign(col_in.begin(), col_in.end());
+        maps.insert(maps.end(), out_slot.begin(), out_slot.end());
+        GTC_CUDA(cudaMemcpyAsync(dmap.get(), maps.data(), maps.size() * 4, cudaMemcpyHostToDevice, s));
+        GTC_CUDA(cudaMemcpyAsync(dps.get(), hps.data(), s_in * sizeof(float), cudaMemcpyHostToDevice, s));
+        A.col_in = dmap.get(), A.out_slot = dmap.get() + s_in;
+        A.s_in = s_in, A.s_out = s_out;
+        A.zin = zc, A.zout = zx;
+        PprLaunch L1 = shape(C, variant, A.w != nullptr);
+        L1.grid1 = std::min(grid1_max, L1.grid1);
+        if (in.timing) tsw.start();
+        run_sweep(C, A, variant, L1, grid2, s);
+        fold(A, L1.grid1 + grid2, out.get(), s);
+        if (in.timing) tsw.stop();
+        L += 3;
+        SL += 3;
+        hout.resize(2 * (size_t)s_in);
+        GTC_CUDA(cudaMemcpyAsync(hout.data(), out.get(), 2 * (size_t)s_in * sizeof(double),
                                  cudaMemcpyDeviceToHost, s));
+        int herr = 0;
+        GTC_CUDA(cudaMemcpyAsync(&herr, derr.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
         GTC_CUDA(cudaStreamSynchronize(s));
-        ++sweep;
-        for (uint32_t b = 0; b < B; ++b) {
-            if (frozen[b]) continue;
-            in.iters[b] = sweep;
-            if (hout[b] < in.params.epsilon ||
-                (in.params.max_iter > 0 && sweep == in.params.max_iter)) {
-                frozen[b] = 1;
+        GTC_REQUIRE(herr == 0, GTC_ERR_CUDA,
+                    "batched personalised PageRank: a gathered row did not arrive in time");
+        if (in.timing) sweep_ms += tsw.ms();
+        ++sweeps;
+        store.clear();
+        for (uint32_t j = 0; j < s_in; ++j) {
+            const uint32_t c = col_in[j];
+            if (c == PPR_NONE || out_slot[j] == PPR_NONE) continue;
+            in.iters[c] = sweeps;
+            psink_col[c] = hout[s_in + j];
+            if (hout[j] < in.params.epsilon ||
+                (in.params.max_iter > 0 && sweeps == in.params.max_iter)) {
+                done[c] = 1;
                 --running;
+                store.push_back(make_uint2(out_slot[j], c));
             }
         }
-        // next sweep's dangling mass per column
-        GTC_CUDA(cudaMemcpyAsync(psink.get(), out.get() + Bp, Bp * sizeof(double),
-                                 cudaMemcpyDeviceToDevice, s));
+        // converged columns go to the output now, from this sweep's iterate
+        // (a copy from pageable memory returns once the source is staged)
+        if (!store.empty() && n) {
+            const uint32_t K = (uint32_t)store.size();
+            GTC_CUDA(cudaMemcpyAsync(dpairs.get(), store.data(), K * sizeof(uint2),
+                                     cudaMemcpyHostToDevice, s));
+            dim3 g2((n + 31) / 32, (K + 31) / 32), blk(32, 8);
+            k_ppr_store<<<g2, blk, 0, s>>>(n, s_out, K, dpairs.get(), g->perm.get(), dinv.get(), zx,
+                                          in.out, in.out_dtype);
+            GTC_LAUNCHED();
+            L++;
+        }
+        col_in = col_out;
+        s_in = s_out;
+        C = c_out;
         std::swap(zc, zx);
     }
     total.stop();
     res->device_ms = total.ms();
-    if (n) {
-        dim3 grid2((n + 31) / 32, (Bp + 31) / 32), blk(32, 8);
-        k_ppr_store<<<grid2, blk, 0, s>>>(n, B, Bp, g->perm.get(), deg.get(), sink.get(), zc,
-                                          in.out, in.out_dtype);
-        GTC_LAUNCHED();
-        L++;
-    }
     GTC_CUDA(cudaStreamSynchronize(s));
-    res->iterations = sweep;
+    res->iterations = sweeps;
     res->last_delta = 0.0;
     res->eigenvalue = 0.0;
     res->launches = L;
-    res->sweep_ms = 0.0;
+    res->sweep_ms = sweep_ms;
     res->sweep_launches = SL;
     g->launches += L;
 }

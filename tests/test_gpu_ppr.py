@@ -42,20 +42,28 @@ def _check(oracle, gtc, n, src, tgt, B, weight=None, reversed=False, eps=1e-7, s
     print(f"ppr batch B={B}: worst rel L1 {worst:.2e}")
 
 
-def test_ppr_batch_matches_separate_solves(oracle, gtc):
+@pytest.fixture(params=["bulk", "regs"])
+def variant(request, monkeypatch):
+    """Both gather variants of the batched sweep (bulk copies into shared
+    memory, loads into registers) must give the oracle's results."""
+    monkeypatch.setenv("GTC_PPR_VARIANT", request.param)
+    return request.param
+
+
+def test_ppr_batch_matches_separate_solves(oracle, gtc, variant):
     from graph_tool import synth
     n, src, tgt, _ = synth.erdos_renyi_sinks(n=3000, m=24000)
     _check(oracle, gtc, n, src, tgt, 37)
 
 
-def test_ppr_batch_padded_columns_weighted(oracle, gtc):
+def test_ppr_batch_padded_columns_weighted(oracle, gtc, variant):
     from graph_tool import synth
     n, src, tgt = synth.rmat_cpu(11, edge_factor=8, seed=4)
     w = np.random.default_rng(2).uniform(0.1, 1.0, src.size)
     _check(oracle, gtc, n, src, tgt, 130, weight=w, seed=3)
 
 
-def test_ppr_batch_reversed_with_hubs(oracle, gtc):
+def test_ppr_batch_reversed_with_hubs(oracle, gtc, variant):
     # a hub with more in-edges than one warp row takes (a CTA row)
     rng = np.random.default_rng(5)
     n, m = 4000, 40000
