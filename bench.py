@@ -285,7 +285,8 @@ def ppr_section(L, device, stream, B=256, sequential=True, scale=22):
     if not sequential:
         _ffi.check(L.gtc_graph_destroy(h))
         return {"batched_ms": t_b, "batched_loop_ms": loop_ms[-1], "batched_sweeps": int(sw[0]),
-                "column_sweeps_mean": float(batch_sweeps.mean())}
+                "column_sweeps_mean": float(batch_sweeps.mean()),
+                "column_sweeps": np.bincount(batch_sweeps.astype(np.int64)).tolist()}
     # B sequential single solves (personalisation vectors prepared beforehand)
     pers = torch.zeros(B, n, dtype=torch.float32, device=device)
     for b, st in enumerate(sets):
@@ -321,6 +322,9 @@ def ppr_section(L, device, stream, B=256, sequential=True, scale=22):
             "speedup_vs_sequential": t_s / t_b, "batched_ms": t_b, "sequential_ms": t_s,
             "batched_sweeps": int(sw[0]), "batched_loop_ms": loop_ms[-1],
             "column_sweeps_mean": float(batch_sweeps.mean()),
+            "column_sweeps_p50_p90_max": [int(np.percentile(batch_sweeps, 50)),
+                                          int(np.percentile(batch_sweeps, 90)),
+                                          int(batch_sweeps.max())],
             "sequential_sweeps_mean": float(np.mean(seq_sweeps)),
             "max_rel_l1_batched_vs_single": max(errs)}
 

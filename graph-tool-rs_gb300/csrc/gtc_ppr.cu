@@ -18,7 +18,9 @@
 // is dropped from the next sweep's output layout: the survivors are packed
 // into the lowest slots, so a sweep reads and writes ceil(active / 32) lines
 // per row, not B / 32.  The sweep that drops a column still gathers it (its
-// input layout is the previous sweep's output layout).
+// input layout is the previous sweep's output layout).  When at most
+// PPR_HANDOFF columns are left, each is finished by the single-vector solver
+// (gtc_centrality.cu) from its current iterate.
 //
 // Schedule.  Rows with more than PPR_CHUNK in-edges are cut into chunks of
 // PPR_CHUNK entries; the first kernel of a sweep runs every chunk (a warp
@@ -53,6 +55,10 @@ constexpr int PPR_WARPS = PPR_NT / 32;
 constexpr uint32_t PPR_CHUNK = 1024;  // rows with more in-edges are cut into chunks
 constexpr uint32_t PPR_MAXB = 512;    // largest batch (16 lines per row)
 constexpr uint32_t PPR_NONE = 0xFFFFFFFFu;
+// At most this many columns left: each is finished by the single-vector
+// solver from its current iterate (a batched sweep of one line costs about
+// as much as this many single-vector sweeps).
+constexpr uint32_t PPR_HANDOFF = 8;
 
 struct PprArgs {
     uint32_t n, s_in, s_out;             // slots per row of zin and zout
@@ -312,7 +318,9 @@ constexpr long long PB_WAIT_CYCLES = 4000000000ll;  // ~2 s: a copy that never l
 constexpr uint32_t PB_BLOCK = 8;                    // rows per plain partial sum
 
 // rows per batch: about 4 KB of rows, 2..32
-constexpr int pb_rows(int C) { return 32 / C >= 2 ? (32 / C > 32 ? 32 : 32 / C) : 2; }
+// rows per batch: 4 KB of rows (more, smaller rings keep more warps resident,
+// which measured faster than fewer warps with longer batches), 2..32
+constexpr int pb_rows(int C) { return 32 / C < 2 ? 2 : 32 / C; }
 
 template <int C>
 struct PbLayout {
@@ -652,6 +660,14 @@ __global__ void k_ppr_store(uint32_t n, uint32_t S, uint32_t K, const uint2* __r
     }
 }
 
+// pers[v] = value, for the seeds of one column in order (the last value
+// given for a vertex wins)
+__global__ void k_ppr_pers(uint32_t k, const uint32_t* __restrict__ verts,
+                           const float* __restrict__ vals, float* __restrict__ pers) {
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        for (uint32_t i = 0; i < k; ++i) pers[verts[i]] = vals[i];
+}
+
 __global__ void k_degree_ppr(uint32_t n, const uint32_t* __restrict__ push_off,
                              const uint32_t* __restrict__ push_eid, const void* __restrict__ w,
                              int wdt, double* __restrict__ deg) {
@@ -888,7 +904,7 @@ int ppr_variant() {
 
 void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* res,
                cudaStream_t s) {
-    uint64_t L = 0, SL = 0;
+    uint64_t L = 0, SL = 0, L_solver = 0;
     const unsigned TB = 256;
     GTC_REQUIRE(!vw || (!vw->vmask && !vw->emask), GTC_ERR_ARG,
                 "batched personalised PageRank supports the graph and its reversal, not filtered "
@@ -1111,14 +1127,65 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
         s_in = s_out;
         C = c_out;
         std::swap(zc, zx);
+        if (running > 0 && running <= PPR_HANDOFF && n) {
+            // the last few columns: their iterates to the output, then the
+            // single-vector solver continues each from there (pagerank_with
+            // from a warm start is the same iteration)
+            const size_t esz = in.out_dtype == GTC_F64 ? 8 : 4;
+            DevBuf<float> pers(n, s), dvals(64, s);
+            DevBuf<uint32_t> dverts(64, s);
+            for (uint32_t j = 0; j < s_in; ++j) {
+                const uint32_t c = col_in[j];
+                if (c == PPR_NONE || done[c]) continue;
+                const uint2 pair = make_uint2(j, c);
+                GTC_CUDA(cudaMemcpyAsync(dpairs.get(), &pair, sizeof(uint2), cudaMemcpyHostToDevice, s));
+                dim3 g2((n + 31) / 32, 1), blk(32, 8);
+                k_ppr_store<<<g2, blk, 0, s>>>(n, s_in, 1, dpairs.get(), g->perm.get(), dinv.get(),
+                                              zc, in.out, in.out_dtype);
+                GTC_LAUNCHED();
+                const uint64_t sb = in.seed_off[c], se = in.seed_off[c + 1];
+                std::vector<uint32_t> hv;
+                std::vector<float> hval;
+                for (uint64_t k = sb; k < se; ++k) {
+                    hv.push_back(in.seed_vertices[k]);
+                    hval.push_back((float)(in.seed_values ? in.seed_values[k] : 1.0 / (double)(se - sb)));
+                }
+                if (hv.size() > dverts.n) dverts.alloc(hv.size(), s), dvals.alloc(hv.size(), s);
+                GTC_CUDA(cudaMemsetAsync(pers.get(), 0, (size_t)n * sizeof(float), s));
+                if (!hv.empty()) {
+                    GTC_CUDA(cudaMemcpyAsync(dverts.get(), hv.data(), hv.size() * 4, cudaMemcpyHostToDevice, s));
+                    GTC_CUDA(cudaMemcpyAsync(dvals.get(), hval.data(), hval.size() * 4, cudaMemcpyHostToDevice, s));
+                    k_ppr_pers<<<1, 32, 0, s>>>((uint32_t)hv.size(), dverts.get(), dvals.get(), pers.get());
+                    GTC_LAUNCHED();
+                }
+                L += 2;
+                SolveIn si{};
+                si.weight = in.weight;
+                si.pers.p = pers.get(), si.pers.len = n, si.pers.dtype = GTC_F32;
+                si.damping = in.damping;
+                si.params = in.params;
+                si.params.max_iter = in.params.max_iter > 0 ? in.params.max_iter - sweeps : 0;
+                si.x = static_cast<char*>(in.out) + (size_t)c * n * esz;
+                si.x_dtype = in.out_dtype;
+                si.had = n;
+                si.precision = GTC_PREC_F32;
+                gtc_result r{};
+                pagerank(g, vw, si, &r, s);
+                in.iters[c] = sweeps + r.iterations;
+                L_solver += r.launches;  // already counted on the handle by the solver
+                SL += r.sweep_launches;
+                done[c] = 1;
+            }
+            running = 0;
+        }
     }
     total.stop();
     res->device_ms = total.ms();
     GTC_CUDA(cudaStreamSynchronize(s));
-    res->iterations = sweeps;
+    res->iterations = B ? *std::max_element(in.iters, in.iters + B) : 0;
     res->last_delta = 0.0;
     res->eigenvalue = 0.0;
-    res->launches = L;
+    res->launches = L + L_solver;
     res->sweep_ms = sweep_ms;
     res->sweep_launches = SL;
     g->launches += L;

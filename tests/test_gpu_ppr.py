@@ -74,6 +74,29 @@ def test_ppr_batch_reversed_with_hubs(oracle, gtc, variant):
     _check(oracle, gtc, n, src.astype(np.uint32), tgt.astype(np.uint32), 64, seed=7, reversed=True)
 
 
+def test_ppr_batch_max_iter_caps_every_column(oracle, gtc, variant):
+    # a cap below convergence: every column stops at the cap with the
+    # iterate of that sweep (also through the single-vector hand-off)
+    from graph_tool import synth
+    n, src, tgt, _ = synth.erdos_renyi_sinks(n=2000, m=16000)
+    rng = np.random.default_rng(9)
+    sets = _seed_sets(n, 20, rng)
+    g = gtc.Graph()
+    g.add_vertex(n)
+    g.add_edges(src, tgt)
+    ranks, iters = g.ppr_batch(sets, epsilon=1e-12, max_iter=5)
+    assert (iters == 5).all()
+    og = oracle.Graph(n)
+    og.add_edge_arrays(src, tgt)
+    for b in (0, 7, 19):
+        pers = np.zeros(n)
+        pers[sets[b]] = 1.0 / len(sets[b])
+        want, it = og.pagerank(pers=pers, epsilon=1e-12, max_iter=5, grain=4096)
+        assert it == 5
+        err = np.abs(ranks[b] - want).sum() / np.abs(want).sum()
+        assert err < 1e-6, (b, err)
+
+
 def test_ppr_batch_rejects_bad_batches(gtc):
     g = gtc.Graph()
     g.add_vertex(3)
