@@ -103,6 +103,46 @@ __global__ void k_degree(uint32_t n, const uint32_t* __restrict__ push_off,
     sink[v] = (act && k == 0.0) ? 1 : 0;
 }
 
+// Merge a compensated partial over the 8 lanes of a lane group (fixed order).
+__device__ __forceinline__ void group8_merge_kahan(Kahan& k) {
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+        const float os = __shfl_xor_sync(0xffffffffu, k.s, o, 8);
+        const float oc = __shfl_xor_sync(0xffffffffu, k.c, o, 8);
+        k.merge(os, oc);
+    }
+}
+
+// The FP32 path's weighted out-degree from the weights gathered in out-half
+// order (wout[p] = w[push_eid[p]]): 8 lanes per vertex (4 vertices per
+// warp), compensated FP32 sums merged in a fixed shuffle order.  (The FP64
+// path keeps the reference's sequential fold above.)  The forward solve and
+// the adjoint both use it, so their degrees have the same bits.
+__global__ void k_degree_f32(uint32_t n, const uint32_t* __restrict__ push_off,
+                             const float* __restrict__ wout, const uint8_t* __restrict__ active,
+                             double* __restrict__ deg, uint8_t* __restrict__ sink) {
+    const uint32_t sub = threadIdx.x & 7;
+    const size_t v = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    const bool in = v < n;  // whole groups leave together: the shuffles stay full-warp
+    Kahan k;
+    if (in) {
+        const uint32_t b = push_off[v], e = push_off[v + 1];
+        uint32_t p = b + sub;
+        for (; p + 24 < e; p += 32) {  // four loads in flight
+            const float x0 = wout[p], x1 = wout[p + 8], x2 = wout[p + 16], x3 = wout[p + 24];
+            k.add(x0), k.add(x1), k.add(x2), k.add(x3);
+        }
+        for (; p < e; p += 8) k.add(wout[p]);
+    }
+    group8_merge_kahan(k);
+    if (in && sub == 0) {
+        const double kd = (double)k.s + (double)k.c;
+        const bool act = !active || active[v];
+        deg[v] = act ? kd : 0.0;
+        sink[v] = (act && kd == 0.0) ? 1 : 0;
+    }
+}
+
 __global__ void k_invdeg_f32(uint32_t n, const double* __restrict__ deg,
                              float* __restrict__ invdeg) {
     size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -114,7 +154,11 @@ template <class T>
 __global__ void k_gather_w(uint32_t m, const uint32_t* __restrict__ eid,
                            const void* __restrict__ w, int wdt, T* __restrict__ out) {
     size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < m) out[p] = (T)ld_any(w, wdt, eid[p]);
+    if (p >= m) return;
+    if (sizeof(T) == 4)
+        out[p] = (T)ld_f32(w, wdt, eid[p]);
+    else
+        out[p] = (T)ld_any(w, wdt, eid[p]);
 }
 
 // Initial iterate (FP64, internal labels): slots below `had` come from the
@@ -133,7 +177,7 @@ __global__ void k_seed(uint32_t n, const uint32_t* __restrict__ perm, uint64_t h
 __global__ void k_to_f32(uint32_t n, const void* __restrict__ x, int xdt,
                          const uint32_t* __restrict__ perm, float* __restrict__ y) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = (float)ld_any(x, xdt, perm ? perm[i] : i);
+    if (i < n) y[i] = ld_f32(x, xdt, perm ? perm[i] : i);
 }
 
 // Store an iterate into the caller's map, in the map's type.  Slots of
@@ -502,7 +546,7 @@ __global__ void k_gather_sw(uint32_t q, const uint32_t* __restrict__ seid, const
     size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p < q) {
         const uint32_t e = seid[p];
-        out[p] = e != 0xFFFFFFFFu ? (float)ld_any(w, wdt, e) : 0.f;
+        out[p] = e != 0xFFFFFFFFu ? ld_f32(w, wdt, e) : 0.f;
     }
 }
 
@@ -536,7 +580,18 @@ void prepare(gtc_graph* g, const gtc_view* vw, const SolveIn& in, bool need_deg,
     if (need_deg) {
         P.deg.alloc(n, s);
         P.sink.alloc(n, s);
-        if (n) {
+        if (n && in.weight.present() && in.precision == GTC_PREC_F32) {
+            const uint32_t mp = P.view.m_pull;  // the push half holds as many entries
+            DevBuf<float> wout(mp, s);
+            if (mp)
+                k_gather_w<float><<<grid_for(mp, TB, 1u << 30), TB, 0, s>>>(
+                    mp, P.view.push_eid, in.weight.p, in.weight.dtype, wout.get());
+            k_degree_f32<<<grid_for((size_t)n * 8, TB, 1u << 30), TB, 0, s>>>(
+                n, P.view.push_off, wout.get(), P.view.active_or_null(), P.deg.get(),
+                P.sink.get());
+            GTC_LAUNCHED();
+            (*L) += 2;
+        } else if (n) {
             k_degree<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(
                 n, P.view.push_off, P.view.push_eid, in.weight.p, in.weight.dtype,
                 P.view.active_or_null(), P.deg.get(), P.sink.get());
@@ -876,10 +931,10 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
 // the PageRank adjoint
 // --------------------------------------------------------------------------
 //
-// Forward fixed point pi = (1-d) p + d (A pi + p (s . pi)), A[t][s] = w_e/deg_s
-// for deg_s != 0 (sinks s contribute through the dangling mass only).  For
-// L(pi) with g = dL/dpi the adjoint lambda solves
-//     lambda = g + d (A^T lambda + s (p . lambda)),
+// Forward fixed point pi = (1-d) p + d M pi, M = A + p s^T, A[t][s] =
+// w_e/deg_s for deg_s != 0 (sinks s contribute through the dangling mass
+// only).  For L(pi) with g = dL/dpi the adjoint lambda solves
+//     lambda = T(lambda) = g + d M^T lambda = g + d (A^T lambda + s (p . lambda)),
 // and (A^T lambda)_s = sum over s's out-edges of (w_e/deg_s) lambda_t, a pull
 // over the out-halves.  By the implicit-function theorem only the converged
 // pi is needed:
@@ -887,51 +942,74 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
 //     dL/dw_e = d (pi_s/deg_s) (lambda_t - (A^T lambda)_s)   (e: s->t, deg_s != 0)
 // (the second term comes from deg_s depending on w_e).  Edges out of a vertex
 // whose weighted degree is 0 get 0 (the map is not differentiable there).
+//
+// Deflation.  With sum(p) = 1, M^T 1 = 1: the all-ones direction is an
+// eigenvector of d M^T with eigenvalue d, so plain iteration from g removes
+// its error only by a factor d per sweep.  The fixed point obeys one exact
+// linear constraint, from the forward system:
+//     (1-d) p . lambda = ((I - d M) pi) . lambda = pi . ((I - d M^T) lambda) = pi . g,
+// so every iterate is shifted along 1 to satisfy p . lambda = tau =
+// (pi . g) / (1-d) before it is swept.  The shift is zero at the fixed point
+// (which is unchanged) and the all-ones error component is re-set from the
+// remaining error at every sweep instead of decaying by d.  The iteration
+// stops when the L1 norm of the fixed-point residual T(lambda) - lambda of
+// the shifted iterate falls below epsilon * |g|_1.
 
-// ptl = p . lambda (deterministic block fold: b = sum)
-__global__ void __launch_bounds__(PR_NT) k_dot(uint32_t n, const float* __restrict__ p,
-                                              float uniform, const float* __restrict__ x,
-                                              Fold2 f) {
-    Kahan acc;
+// (sum_v a_v x_v, sum_v b_v y_v) over n entries: a null a or b is the
+// constant ua / ub, a null x or y is 1; `absy` sums |b_v y_v|.  Deterministic
+// block fold into (out_a, out_b).
+__global__ void __launch_bounds__(PR_NT) k_dot2(uint32_t n, const float* __restrict__ a, float ua,
+                                               const float* __restrict__ x,
+                                               const float* __restrict__ b, float ub,
+                                               const float* __restrict__ y, bool absy, Fold2 f) {
+    Kahan ka, kb;
     for (size_t v = (size_t)blockIdx.x * PR_NT + threadIdx.x; v < n;
-         v += (size_t)gridDim.x * PR_NT)
-        acc.add(__fmul_rn(p ? p[v] : uniform, x[v]));
-    block_fold2<PR_NT>(0.0, (double)acc.s + (double)acc.c, f);
+         v += (size_t)gridDim.x * PR_NT) {
+        ka.add(__fmul_rn(a ? a[v] : ua, x ? x[v] : 1.f));
+        const float t = __fmul_rn(b ? b[v] : ub, y ? y[v] : 1.f);
+        kb.add(absy ? fabsf(t) : t);
+    }
+    block_fold2<PR_NT>((double)ka.s + (double)ka.c, (double)kb.s + (double)kb.c, f);
 }
 
-// grad_p[v] = lambda[iperm v] * c (original labels)
+// grad_p[v] = (lambda + alpha)[iperm v] * c (original labels)
 __global__ void k_grad_pers(uint32_t n, const uint32_t* __restrict__ iperm,
-                            const float* __restrict__ lam, const double* __restrict__ psink_pi,
-                            double one_minus_d, double d, void* __restrict__ out, int dt) {
+                            const float* __restrict__ lam, float alpha,
+                            const double* __restrict__ psink_pi, double one_minus_d, double d,
+                            void* __restrict__ out, int dt) {
     size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
-    const double c = one_minus_d + d * (*psink_pi);
-    const double gv = (double)lam[iperm[v]] * c;
+    const float c = (float)(one_minus_d + d * (*psink_pi));
+    const float gv = __fmul_rn(__fadd_rn(lam[iperm[v]], alpha), c);
     if (dt == GTC_F64)
-        ((double*)out)[v] = gv;
+        ((double*)out)[v] = (double)gv;
     else
-        ((float*)out)[v] = (float)gv;
+        ((float*)out)[v] = gv;
 }
 
-// grad_w over the out-half entries: thread per entry, its row by binary search
-__global__ void k_grad_w(uint32_t n, uint32_t m, const uint32_t* __restrict__ off,
+// rowid[p] = s for the entries p of row s (8 lanes per row).
+__global__ void k_row_ids(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ rowid) {
+    const uint32_t sub = threadIdx.x & 7;
+    const size_t s = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    if (s >= n) return;
+    for (uint32_t p = off[s] + sub, e = off[s + 1]; p < e; p += 8) rowid[p] = (uint32_t)s;
+}
+
+// grad_w over the out-half entries (a thread each, its row from rowid):
+// d (pi_s / deg_s) (lambda_t - (A^T lambda)_s) with lambda = lam + alpha_K
+// and A^T lambda = atl + alpha_{K-1} (the last sweep's): dalpha = the
+// difference of the two shifts.
+__global__ void k_grad_w(uint32_t m, const uint32_t* __restrict__ rowid,
                          const uint32_t* __restrict__ other, const uint32_t* __restrict__ eid,
                          const float* __restrict__ y, const float* __restrict__ lam,
-                         const float* __restrict__ atl, const double* __restrict__ deg, float d,
-                         void* __restrict__ out, int dt) {
-    size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+                         const float* __restrict__ atl, const uint8_t* __restrict__ sink, float d,
+                         float dalpha, void* __restrict__ out, int dt) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= m) return;
-    uint32_t lo = 0, hi = n;  // last row with off[row] <= p
-    while (hi - lo > 1) {
-        const uint32_t mid = lo + (hi - lo) / 2;
-        if (off[mid] <= (uint32_t)p)
-            lo = mid;
-        else
-            hi = mid;
-    }
-    const uint32_t s = lo;
-    float gw = 0.f;
-    if (deg[s] != 0.0) gw = __fmul_rn(__fmul_rn(d, y[s]), __fsub_rn(lam[other[p]], atl[s]));
+    const uint32_t s = rowid[p];
+    const float gw = sink[s] ? 0.f
+                             : __fmul_rn(__fmul_rn(d, y[s]),
+                                         __fsub_rn(lam[other[p]], __fsub_rn(atl[s], dalpha)));
     const uint32_t e = eid[p];
     if (dt == GTC_F64)
         ((double*)out)[e] = (double)gw;
@@ -952,10 +1030,36 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     fin.x = const_cast<void*>(in.pi.p);
     fin.x_dtype = in.pi.dtype;
     fin.had = g->n;  // pi is the seed: x64 = pi (internal labels)
+    fin.precision = GTC_PREC_F32;
+    const bool W = in.weight.present();
     Prep P;
-    prepare(g, vw, fin, true, P, s, &L);
+    // weighted: the degrees come from the out-half weights gathered below
+    prepare(g, vw, fin, !W, P, s, &L);
     const uint32_t n = P.view.n;
     const double d = in.damping;
+    // the adjoint pulls over the forward view's out-halves: the reversed view
+    gtc_view rv{};
+    rv.reversed = (vw && vw->reversed) ? 0 : 1;
+    View av;
+    av.prepare(g, &rv, s, &L);
+    DevBuf<float> wpull;
+    if (W && av.m_pull) {
+        wpull.alloc(av.m_pull, s);
+        k_gather_w<float><<<grid_for(av.m_pull, 256, 1u << 30), 256, 0, s>>>(
+            av.m_pull, av.pull_eid, in.weight.p, in.weight.dtype, wpull.get());
+        GTC_LAUNCHED();
+        L++;
+    }
+    if (W) {
+        P.deg.alloc(n, s);
+        P.sink.alloc(n, s);
+        if (n) {
+            k_degree_f32<<<grid_for((size_t)n * 8, TB, 1u << 30), TB, 0, s>>>(
+                n, av.pull_off, wpull.get(), nullptr, P.deg.get(), P.sink.get());
+            GTC_LAUNCHED();
+            L++;
+        }
+    }
     DevBuf<float> invdeg(n, s), pers32, g32(n, s), pi32(n, s), ypi((size_t)n + 1, s);
     if (n) {
         k_invdeg_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.deg.get(), invdeg.get());
@@ -974,42 +1078,38 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     }
     const unsigned nb = persistent_blocks(n);
     FoldBufs fb(nb, s);
-    double* dp = fb.out.get();  // [1] dangling mass of pi, [3] p . lambda0
+    double* dp = fb.out.get();  // [1] dangling mass of pi
     // y = pi / deg and the dangling mass of pi
     k_pr_prime<<<nb, PR_NT, 0, s>>>(n, pi32.get(), invdeg.get(), P.sink.get(), ypi.get(),
                                    fb.fold(dp + 2, dp + 1));
     GTC_LAUNCHED();
     L++;
 
-    // the adjoint pulls over the forward view's out-halves: the reversed view
-    gtc_view rv{};
-    rv.reversed = (vw && vw->reversed) ? 0 : 1;
-    View av;
-    av.prepare(g, &rv, s, &L);
     Units local;
     Units* U = pull_units(g, av, local, s);
-    const bool W = in.weight.present();
-    DevBuf<float> wpull;
-    if (W && av.m_pull) {
-        wpull.alloc(av.m_pull, s);
-        k_gather_w<float><<<grid_for(av.m_pull, 256, 1u << 30), 256, 0, s>>>(
-            av.m_pull, av.pull_eid, in.weight.p, in.weight.dtype, wpull.get());
-        GTC_LAUNCHED();
-        L++;
-    }
     DevBuf<float> lam0((size_t)n + 1, s), lam1((size_t)n + 1, s), atl((size_t)n + 1, s);
     GTC_CUDA(cudaMemsetAsync(lam0.get() + n, 0, sizeof(float), s));
     GTC_CUDA(cudaMemsetAsync(lam1.get() + n, 0, sizeof(float), s));
     if (n) GTC_CUDA(cudaMemcpyAsync(lam0.get(), g32.get(), (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    // p . g, pi . g, sum(p), |g|_1
     FoldBufs fd(nb, s);
-    k_dot<<<nb, PR_NT, 0, s>>>(n, pers32.get(), (float)P.uniform, lam0.get(),
-                              fd.fold(fd.out.get() + 2, fd.out.get() + 3));
+    const float uni = (float)P.uniform;
+    k_dot2<<<nb, PR_NT, 0, s>>>(n, pers32.get(), uni, g32.get(), pi32.get(), 0.f, g32.get(), false,
+                               fd.fold(fd.out.get(), fd.out.get() + 1));
+    k_dot2<<<nb, PR_NT, 0, s>>>(n, pers32.get(), uni, nullptr, nullptr, 1.f, g32.get(), true,
+                               fd.fold(fd.out.get() + 2, fd.out.get() + 3));
     GTC_LAUNCHED();
-    L++;
-    FoldBufs fs(1, s);
-    double* dq = fs.out.get();  // [0] delta, [1] p . lambda of the current iterate
-    GTC_CUDA(cudaMemcpyAsync(dq + 1, fd.out.get() + 3, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    L += 2;
+    double h4[4] = {0, 0, 0, 0};
+    GTC_CUDA(cudaMemcpyAsync(h4, fd.out.get(), sizeof(h4), cudaMemcpyDeviceToHost, s));
+    GTC_CUDA(cudaStreamSynchronize(s));
+    const double psum = h4[2], gnorm = h4[3];
+    const bool deflate = psum > 0.0 && d < 1.0;
+    double tau = deflate ? h4[1] / (1.0 - d) : h4[0];  // without deflation: p . lambda
+    double alpha = deflate ? (tau - h4[0]) / psum : 0.0, alpha_prev = alpha;
 
+    FoldBufs fs(1, s);
+    double* dq = fs.out.get();  // [0] residual, [1] p . (next iterate before its shift)
     SweepArgs A{};
     set_schedule(A, *U, av);
     DevBuf<float> swt = sliced_weights(*U, fin, s, &L);
@@ -1019,53 +1119,67 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     A.sink = P.sink.get();
     A.pers = pers32.get();
     A.gvec = g32.get();
-    A.uniform = (float)P.uniform;
+    A.uniform = uni;
     A.one_minus_d = (float)(1.0 - d);
     A.d = (float)d;
-    A.psink = dq + 1;
+    A.psink = dq + 1;  // read but unused in this mode
+    A.alpha = (float)alpha;
+    A.tau = (float)tau;
     A.ticket = fs.ticket.get();
     A.out = dq;
     A.ynext = atl.get();
     float *lc = lam0.get(), *ln = lam1.get();
     A.x = lc, A.prev = lc, A.next = ln;
     const int var = tuned_variant<MODE_ADJOINT>(*U, A, W, s, &L);
-    GTC_CUDA(cudaMemcpyAsync(dq + 1, fd.out.get() + 3, sizeof(double), cudaMemcpyDeviceToDevice, s));
 
     const uint64_t max_iter = in.params.max_iter;
-    const double eps = in.params.epsilon;
+    const double tol = in.params.epsilon * gnorm;
     uint64_t iter = 0;
-    double delta = eps + 1.0, sweep_ms = 0.0;
+    double delta = tol + 1.0, sweep_ms = 0.0;
     Timer total(s), sw(s);
     total.start();
-    while (delta >= eps) {
+    // g = 0 gives lambda = 0 (the start) and no sweep; a NaN stops at once
+    while (gnorm > 0.0 && delta >= tol) {
         A.x = lc, A.prev = lc, A.next = ln;
+        A.alpha = (float)alpha;
+        A.tau = (float)tau;
         if (in.timing) sw.start();
         launch_sweep<MODE_ADJOINT>(var, A, W, s);
         if (in.timing) sw.stop();
         L++;
         SL++;
-        GTC_CUDA(cudaMemcpyAsync(&delta, dq, sizeof(double), cudaMemcpyDeviceToHost, s));
+        double h2[2];
+        GTC_CUDA(cudaMemcpyAsync(h2, dq, sizeof(h2), cudaMemcpyDeviceToHost, s));
         GTC_CUDA(cudaStreamSynchronize(s));
         if (in.timing) sweep_ms += sw.ms();
+        delta = h2[0];
+        alpha_prev = alpha;
+        if (deflate)
+            alpha = (tau - h2[1]) / psum;
+        else
+            tau = h2[1];
         std::swap(lc, ln);
         iter++;
         if (max_iter > 0 && iter == max_iter) break;
     }
     total.stop();
     res->device_ms = total.ms();
-    // gradients
+    // gradients, with lambda = lc + alpha
     if (in.grad_p && n) {
-        k_grad_pers<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->iperm.get(), lc, dp + 1, 1.0 - d,
-                                                             d, in.grad_p, in.grad_p_dtype);
+        k_grad_pers<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->iperm.get(), lc, (float)alpha,
+                                                             dp + 1, 1.0 - d, d, in.grad_p,
+                                                             in.grad_p_dtype);
         GTC_LAUNCHED();
         L++;
     }
     if (in.grad_w && av.m_pull) {
+        DevBuf<uint32_t> rowid(av.m_pull, s);
+        k_row_ids<<<grid_for((size_t)n * 8, TB, 1u << 30), TB, 0, s>>>(n, av.pull_off, rowid.get());
         k_grad_w<<<grid_for(av.m_pull, TB, 1u << 30), TB, 0, s>>>(
-            n, av.m_pull, av.pull_off, av.pull_other, av.pull_eid, ypi.get(), lc, atl.get(),
-            P.deg.get(), (float)d, in.grad_w, in.grad_w_dtype);
+            av.m_pull, rowid.get(), av.pull_other, av.pull_eid, ypi.get(), lc, atl.get(),
+            P.sink.get(), (float)d, (float)(alpha - alpha_prev), in.grad_w, in.grad_w_dtype);
         GTC_LAUNCHED();
-        L++;
+        L += 2;
     }
     GTC_CUDA(cudaStreamSynchronize(s));
     res->iterations = iter;

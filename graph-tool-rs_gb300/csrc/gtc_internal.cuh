@@ -186,6 +186,13 @@ __device__ __forceinline__ double ld_any(const void* p, int dtype, size_t i) {
     return dtype == GTC_F64 ? ((const double*)p)[i] : (double)((const float*)p)[i];
 }
 
+// The same as FP32: an FP32 input is read as is, so no conversion runs on
+// the FP64 pipe (on this GPU a conversion per element costs more than the
+// element's memory traffic).
+__device__ __forceinline__ float ld_f32(const void* p, int dtype, size_t i) {
+    return dtype == GTC_F64 ? (float)((const double*)p)[i] : ((const float*)p)[i];
+}
+
 // Inputs of the PageRank adjoint (device vectors, original labels).
 struct AdjointIn {
     DVec weight, pers;           // as the forward solve

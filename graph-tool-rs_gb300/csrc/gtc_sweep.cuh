@@ -84,7 +84,8 @@ struct SweepArgs {
     const float* __restrict__ pers;     // PageRank / adjoint (null = uniform)
     const float* __restrict__ gvec;     // adjoint: dL/dpi
     float uniform, one_minus_d, d;
-    const double* psink;                // PageRank: dangling mass of prev; adjoint: p . prev
+    const double* psink;                // PageRank: dangling mass of prev
+    float alpha, tau;                   // adjoint: shift of the iterate, p . (shifted iterate)
     // reduction: every item's terms, folded by the last CTA
     unsigned* ticket;
     double* out;  // [a, b]
@@ -131,15 +132,19 @@ __device__ __forceinline__ void sweep_row(const SweepArgs& A, uint32_t v, float 
         ta = fabsf(__fsub_rn(nv, __ldcs(A.prev + v)));
         tb = __ldcs(A.sink + v) ? nv : 0.f;
     } else if (MODE == MODE_ADJOINT) {
-        // sum = sum over v's out-edges of w * lambda[t]; A^T lambda = sum / deg
+        // The iterate is mu + alpha (a shift along the all-ones vector, which
+        // the transposed map keeps: A^T 1 = 1 off the sinks).  sum = sum over
+        // v's out-edges of w * mu[t], so (A^T (mu + alpha))_v = at + alpha off
+        // the sinks, and a sink takes p . (mu + alpha) = tau.
         const float at = __fmul_rn(__ldcs(A.invdeg + v), sum);
-        const float dn = __ldcs(A.sink + v) ? __fadd_rn(at, psink) : at;
+        const float dn = __fadd_rn(at, __ldcs(A.sink + v) ? A.tau : A.alpha);
         const float nv = __fadd_rn(__ldcs(A.gvec + v), __fmul_rn(A.d, dn));
         __stcs(A.next + v, nv);
         A.ynext[v] = at;  // kept for the weight gradient
-        ta = fabsf(__fsub_rn(nv, __ldcs(A.prev + v)));
+        // the fixed-point residual of the shifted iterate
+        ta = fabsf(__fsub_rn(__fsub_rn(nv, __ldcs(A.prev + v)), A.alpha));
         const float pv = A.pers ? __ldcs(A.pers + v) : A.uniform;
-        tb = __fmul_rn(pv, nv);  // next sweep's p . lambda
+        tb = __fmul_rn(pv, nv);  // p . (next iterate, before its shift)
     } else {
         A.next[v] = sum;
         ta = __fmul_rn(sum, sum);

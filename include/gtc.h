@@ -234,7 +234,10 @@ int gtc_ppr_batch_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* wei
  * The adjoint of PageRank (no counterpart in the reference, which has no
  * differentiation): for a scalar L(pi) of the converged PageRank pi, with
  * grad_pi = dL/dpi, solve lambda = grad_pi + d (A^T lambda + s (p . lambda))
- * (A^T pulled over the out-halves, s the dangling vertices) to epsilon, then
+ * (A^T pulled over the out-halves, s the dangling vertices) until the L1 norm
+ * of the fixed-point residual is below epsilon * |grad_pi|_1 (the iterate is
+ * kept on the exact constraint p . lambda = (pi . grad_pi) / (1 - d), which
+ * removes the slowest error mode), then
  *   grad_pers[v]   = lambda_v ((1-d) + d (s . pi))
  *   grad_weight[e] = d (pi_s / deg_s) (lambda_t - (A^T lambda)_s)   e: s -> t
  * (0 for edges out of a vertex of zero weighted degree).  Only the converged
