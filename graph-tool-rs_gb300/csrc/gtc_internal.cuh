@@ -151,6 +151,7 @@ struct gtc_graph {
     gtc::Halves in;   // CSC: in-halves (in_edges order, the pull order)
     gtc::Units units_in, units_out;  // pull schedules of the plain and reversed views
     gtc::PprSched ppr_sched[2];      // batched schedules of the plain and reversed views
+    gtc::DevBuf<float> ppr_z[2];     // batched iterates, kept between calls (grown on demand)
     uint64_t launches = 0;  // kernels this handle has launched (diagnostics)
 };
 

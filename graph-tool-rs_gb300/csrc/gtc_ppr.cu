@@ -6,7 +6,7 @@
 // each stopping at the first sweep whose L1 change falls below epsilon
 // (centrality.rs:372-381), its value the iterate of that sweep.
 //
-// Layout.  Z is [n x S] row-major, S = 32 * C slots (C = 1-4, 8, 12 or 16
+// Layout.  Z is [n x S] row-major, S = 32 * C slots (C = 1-4, 6, 8, 12 or 16
 // lines of 128 bytes); a warp reads a row with C / V coalesced vector loads
 // of V floats per lane (Lanes<C>).  Z[v][j]
 // holds rank_b[v] / deg_v of the column b in slot j for a vertex with
@@ -862,8 +862,8 @@ void fold(const PprArgs& A, unsigned n_parts, double* out, cudaStream_t s) {
     GTC_LAUNCHED();
 }
 
-// line counts a sweep runs at: 1-4, then multiples of 4 (vector loads)
-#define GTC_PPR_C(X) X(1) X(2) X(3) X(4) X(8) X(12) X(16)
+// line counts a sweep runs at: 1-4, 6, then multiples of 4 (vector loads)
+#define GTC_PPR_C(X) X(1) X(2) X(3) X(4) X(6) X(8) X(12) X(16)
 
 PprLaunch shape(uint32_t C, int variant, bool weighted) {
     switch (C) {
@@ -886,11 +886,11 @@ void run_sweep(uint32_t C, const PprArgs& A, int variant, const PprLaunch& L1, u
     throw Error{GTC_ERR_CUDA, "batched personalised PageRank: bad slot count"};
 }
 
-// Lines per row for `active` columns: ceil(active / 32), rounded up to a
-// multiple of 4 above 4 lines.
+// Lines per row for `active` columns: ceil(active / 32), rounded up to 6 or
+// to a multiple of 4 above 4 lines (widths with vector loads).
 inline uint32_t ppr_lines(uint32_t active) {
     const uint32_t c = (active + 31) / 32;
-    return c <= 4 ? c : (c + 3) / 4 * 4;
+    return c <= 4 ? c : (c <= 6 ? 6 : (c + 3) / 4 * 4);
 }
 
 // GTC_PPR_VARIANT=regs|bulk pins the gather variant (default bulk).
@@ -1010,7 +1010,16 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     uint32_t C = ppr_lines(B);
     uint32_t s_in = 32 * C;
     const size_t zn = (size_t)n * s_in;
-    DevBuf<float> z0(zn, s), z1(zn, s);
+    // the two iterate buffers live on the handle: a later batch of the same
+    // or a smaller width does not allocate them again
+    if (g->ppr_z[0].n < zn || !g->ppr_z[0].get()) {
+        GTC_CUDA(cudaStreamSynchronize(s));
+        g->ppr_z[0].alloc(zn, g->home);
+        g->ppr_z[1].alloc(zn, g->home);
+        GTC_CUDA(cudaStreamSynchronize(g->home));
+    }
+    DevBuf<float>& z0 = g->ppr_z[0];
+    DevBuf<float>& z1 = g->ppr_z[1];
     if (zn) GTC_CUDA(cudaMemsetAsync(z0.get(), 0, zn * sizeof(float), s));
     if (nu && n) {
         k_ppr_init<<<grid_for(nu, TB, 1u << 30), TB, 0, s>>>(nu, s_in, dsv.get(), dsd.get(),

@@ -215,7 +215,10 @@ int gtc_eigenvector_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* w
  * centrality.rs:198-205) and stops at the first sweep whose L1 change is
  * below params->epsilon (or at max_iter); iters[b] receives its sweep count.
  * ranks is [B][n] (row b = vector b, by vertex index).  1 <= B <= 512.
- * GTC_PREC_F32; plain or reversed views.  Host arrays except as named. */
+ * GTC_PREC_F32; plain or reversed views.  Host arrays except as named.
+ * The handle keeps two iterate buffers of n x 32 ceil(B / 32) floats between
+ * calls (released by gtc_graph_destroy); batched calls on one handle must
+ * not overlap. */
 int gtc_ppr_batch(gtc_graph* g, const gtc_view* view, const double* weight, uint64_t weight_len,
                   uint32_t B, const uint64_t* seed_off, const uint32_t* seed_vertices,
                   const double* seed_values, double damping, const gtc_power_iteration* params,
