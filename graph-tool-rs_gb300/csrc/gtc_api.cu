@@ -2,6 +2,8 @@
 // handle lifetime.  Every entry point catches everything; nothing unwinds
 // into the caller.
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <algorithm>
 #include <new>
@@ -23,6 +25,9 @@ static void require_device() {
                     std::string("no usable CUDA device: ") +
                         (e != cudaSuccess ? cudaGetErrorString(e) : "device count is 0")};
     }
+    e = cudaFree(nullptr);  // the device's context exists before any handle is made
+    if (e != cudaSuccess)
+        throw Error{GTC_ERR_CUDA, std::string("context creation failed: ") + cudaGetErrorString(e)};
 }
 
 template <class F>
@@ -49,9 +54,7 @@ static gtc_graph* new_graph(uint64_t n, uint64_t m) {
     GTC_REQUIRE(m <= 0xFFFFFFFEull, GTC_ERR_ARG,
                 "edge count exceeds the index space (MAX_INDEX = 2^32 - 2)");
     require_device();
-    gtc_graph* g = new gtc_graph();
-    g->n = (uint32_t)n;
-    g->m = (uint32_t)m;
+    gtc_graph* g = new gtc_graph((uint32_t)n, (uint32_t)m);
     cudaError_t e = cudaGetDevice(&g->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->home, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -59,6 +62,22 @@ static gtc_graph* new_graph(uint64_t n, uint64_t m) {
         throw Error{GTC_ERR_CUDA, std::string("stream creation failed: ") + cudaGetErrorString(e)};
     }
     g->stream = g->home;
+    // The sizes are stored once more and read back: on GB300 hosts the first
+    // handle of a process was seen to lose the constructor's store of m (it
+    // read 0 right after construction, in heap or mmap'd memory alike),
+    // which turned the first solve into one over an edgeless graph.
+    volatile uint32_t* vn = &g->n;
+    volatile uint32_t* vm = &g->m;
+    for (int k = 0; k < 3 && (*vn != (uint32_t)n || *vm != (uint32_t)m); ++k) {
+        *vn = (uint32_t)n;
+        *vm = (uint32_t)m;
+        __atomic_thread_fence(__ATOMIC_SEQ_CST);
+    }
+    if (*vn != (uint32_t)n || *vm != (uint32_t)m) {
+        cudaStreamDestroy(g->home);
+        delete g;
+        throw Error{GTC_ERR_CUDA, "the graph handle did not keep its sizes (internal error)"};
+    }
     return g;
 }
 

@@ -134,9 +134,51 @@ struct PprSched {
     bool built = false;
 };
 
+// Segmented pull plan of one unfiltered view (gtc_seg.cu): entries sorted by
+// (source segment, destination group, destination), pair sums per
+// (segment, destination), kept with the graph.
+struct SegPlan {
+    uint32_t n = 0, m = 0, nseg = 0, ngroups = 0, npairs = 0, nunits = 0, nitems = 0;
+    DevBuf<uint16_t> src16;           // per entry: local source | pair start << 15
+    DevBuf<uint32_t> seid;            // per entry: edge id (weights are gathered through it)
+    DevBuf<uint32_t> unit_e, unit_o;  // per unit: first entry (+1 end), output of its first pair
+    DevBuf<uint4> items;              // phase-1 CTA items {segment, first unit, end unit, 0}
+    DevBuf<uint16_t> pdest;           // per pair (group order): local destination | run start << 15
+    DevBuf<uint32_t> gpair;           // per destination group: first pair (ngroups + 1)
+    DevBuf<float> partial;            // per pair: the sweep's pair sums (scratch)
+    int choice[2] = {-1, -1};         // tuned per [weighted]: 1 = the segmented sweep is faster
+    bool built = false;
+};
+
+// Arguments of one segmented PageRank sweep.
+struct SegArgs {
+    uint32_t n, ngroups, nitems;
+    const uint16_t* src16;
+    const float* ws;        // weights in entry order, or null
+    const float* y;         // rank / deg of the current iterate
+    const uint32_t *unit_e, *unit_o;
+    const uint4* items;
+    float* partial;
+    const uint16_t* pdest;
+    const uint32_t* gpair;
+    const float* pers;      // null: uniform
+    float uniform, one_minus_d, d;
+    const double* psink;    // dangling mass of the current iterate
+    const float* prev;
+    float* next;
+    float* ynext;
+    const float* invdeg;
+    const uint8_t* sink;
+    double* part;           // per phase-2 CTA: (change, dangling mass)
+    unsigned* ticket;
+    double* out;            // [0] L1 change, [1] dangling mass of next
+};
+
 }  // namespace gtc
 
 struct gtc_graph {
+    gtc_graph() = default;
+    gtc_graph(uint32_t n_, uint32_t m_) : n(n_), m(m_) {}
     int device = 0;
     uint32_t n = 0;  // vertex bound
     uint32_t m = 0;  // edge bound == live edges (ids 0..m-1)
@@ -152,6 +194,7 @@ struct gtc_graph {
     gtc::Units units_in, units_out;  // pull schedules of the plain and reversed views
     gtc::PprSched ppr_sched[2];      // batched schedules of the plain and reversed views
     gtc::DevBuf<float> ppr_z[2];     // batched iterates, kept between calls (grown on demand)
+    gtc::SegPlan seg[2];             // segmented pull plans of the plain and reversed views
     uint64_t launches = 0;  // kernels this handle has launched (diagnostics)
 };
 
@@ -193,6 +236,14 @@ __device__ __forceinline__ double ld_any(const void* p, int dtype, size_t i) {
 __device__ __forceinline__ float ld_f32(const void* p, int dtype, size_t i) {
     return dtype == GTC_F64 ? (float)((const double*)p)[i] : ((const float*)p)[i];
 }
+
+// segmented pull sweep (gtc_seg.cu)
+struct View;
+bool seg_supported(const View& view);
+void build_seg(gtc_graph* g, const View& view, cudaStream_t s, SegPlan& P);
+void seg_gather_weights(const SegPlan& P, const DVec& w, float* ws, cudaStream_t s);
+void seg_sweep(const SegPlan& P, SegArgs A, bool weighted, cudaStream_t s);
+uint32_t seg_part_slots(const SegPlan& P);
 
 // Inputs of the PageRank adjoint (device vectors, original labels).
 struct AdjointIn {
