@@ -515,4 +515,139 @@ int gtc_ppr_batch(gtc_graph* g, const gtc_view* view, const double* weight, uint
     });
 }
 
+
+static void destroy_batch(gtc_graph_batch* b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    gtc_graph* u = b->u;
+    b->u = nullptr;
+    delete b;  // its buffers are freed on the union's home stream
+    destroy_graph(u);
+}
+
+int gtc_graph_batch_create(uint64_t G, const uint64_t* voff, const uint64_t* eoff,
+                           const uint32_t* src, const uint32_t* tgt, gtc_graph_batch** out) {
+    return guarded([&] {
+        GTC_REQUIRE(out, GTC_ERR_ARG, "out is NULL");
+        *out = nullptr;
+        GTC_REQUIRE(G >= 1 && G < (1ull << 31), GTC_ERR_ARG, "a batch holds 1 to 2^31 - 1 graphs");
+        GTC_REQUIRE(voff && eoff, GTC_ERR_ARG, "voff/eoff is NULL");
+        GTC_REQUIRE(voff[0] == 0 && eoff[0] == 0, GTC_ERR_ARG, "voff[0] and eoff[0] must be 0");
+        for (uint64_t k = 0; k < G; ++k) {
+            GTC_REQUIRE(voff[k + 1] >= voff[k] && eoff[k + 1] >= eoff[k], GTC_ERR_ARG,
+                        "voff/eoff must not decrease");
+        }
+        const uint64_t n = voff[G], m = eoff[G];
+        GTC_REQUIRE(n <= 0xFFFFFFFEull && m <= 0xFFFFFFFEull, GTC_ERR_ARG,
+                    "the packed batch exceeds the index space (MAX_INDEX = 2^32 - 2)");
+        GTC_REQUIRE(m == 0 || (src && tgt), GTC_ERR_ARG, "src/tgt is NULL");
+        // endpoints to packed labels, checked against their own graph
+        std::vector<uint32_t> gs(m), gt(m);
+        for (uint64_t k = 0; k < G; ++k) {
+            const uint64_t nk = voff[k + 1] - voff[k];
+            for (uint64_t e = eoff[k]; e < eoff[k + 1]; ++e) {
+                GTC_REQUIRE(src[e] < nk && tgt[e] < nk, GTC_ERR_ARG,
+                            "add_edge: no such vertex (an endpoint is >= its graph's n)");
+                gs[e] = (uint32_t)(src[e] + voff[k]);
+                gt[e] = (uint32_t)(tgt[e] + voff[k]);
+            }
+        }
+        gtc_graph_batch* b = new gtc_graph_batch();
+        try {
+            b->u = new_graph(n, m);
+            b->G = (uint32_t)G;
+            cudaStream_t h = b->u->home;
+            {
+                DevBuf<uint32_t> ds(m, h), dt(m, h);
+                if (m) {
+                    GTC_CUDA(cudaMemcpyAsync(ds.get(), gs.data(), m * 4, cudaMemcpyHostToDevice, h));
+                    GTC_CUDA(cudaMemcpyAsync(dt.get(), gt.data(), m * 4, cudaMemcpyHostToDevice, h));
+                }
+                build_halves(b->u, ds.get(), dt.get(), /*relabel=*/false);
+            }
+            b->hvoff.resize(G + 1);
+            b->heoff.resize(G + 1);
+            for (uint64_t k = 0; k <= G; ++k) b->hvoff[k] = (uint32_t)voff[k], b->heoff[k] = (uint32_t)eoff[k];
+            std::vector<uint32_t> order(G);
+            for (uint32_t k = 0; k < G; ++k) order[k] = k;
+            std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c) {
+                return (eoff[a + 1] - eoff[a]) + (voff[a + 1] - voff[a]) >
+                       (eoff[c + 1] - eoff[c]) + (voff[c + 1] - voff[c]);
+            });
+            b->voff.alloc(G + 1, h);
+            b->order.alloc(G, h);
+            GTC_CUDA(cudaMemcpyAsync(b->voff.get(), b->hvoff.data(), (G + 1) * 4, cudaMemcpyHostToDevice, h));
+            GTC_CUDA(cudaMemcpyAsync(b->order.get(), order.data(), G * 4, cudaMemcpyHostToDevice, h));
+            GTC_CUDA(cudaStreamSynchronize(h));
+        } catch (...) {
+            destroy_batch(b);
+            throw;
+        }
+        *out = b;
+    });
+}
+
+int gtc_graph_batch_destroy(gtc_graph_batch* b) {
+    return guarded([&] { destroy_batch(b); });
+}
+
+int gtc_graph_batch_info(const gtc_graph_batch* b, uint64_t* graphs, uint64_t* vertices,
+                         uint64_t* edges) {
+    return guarded([&] {
+        GTC_REQUIRE(b, GTC_ERR_ARG, "batch is NULL");
+        if (graphs) *graphs = b->G;
+        if (vertices) *vertices = b->u->n;
+        if (edges) *edges = b->u->m;
+    });
+}
+
+int gtc_pagerank_batch_device(gtc_graph_batch* b, const gtc_dvec* weight, double damping,
+                              double epsilon, uint64_t max_iter, gtc_dvec* rank, uint64_t* iters,
+                              const gtc_options* opt, gtc_result* result) {
+    return guarded([&] {
+        GTC_REQUIRE(b, GTC_ERR_ARG, "batch is NULL");
+        GTC_REQUIRE(!std::isnan(damping) && !std::isnan(epsilon), GTC_ERR_ARG,
+                    "damping or epsilon is NaN");
+        GTC_REQUIRE(!opt || opt->precision == GTC_PREC_F32, GTC_ERR_ARG,
+                    "batched PageRank runs in GTC_PREC_F32");
+        const DVec w = dvec_in(weight, b->u->m, "weight");
+        GTC_REQUIRE(rank && (rank->ptr || b->u->n == 0), GTC_ERR_ARG, "rank is NULL");
+        GTC_REQUIRE(rank->len >= b->u->n, GTC_ERR_ARG, "rank holds fewer entries than the batch's vertices");
+        GTC_REQUIRE(rank->dtype == GTC_F64 || rank->dtype == GTC_F32, GTC_ERR_ARG, "rank: unknown dtype");
+        gtc_result r{};
+        gtc::pagerank_batch(b, w, damping, epsilon, max_iter, rank->ptr, rank->dtype, iters,
+                            opt && opt->timing, &r, stream_of(b->u, opt));
+        if (result) *result = r;
+    });
+}
+
+int gtc_pagerank_batch(gtc_graph_batch* b, const double* weight, uint64_t weight_len,
+                       double damping, double epsilon, uint64_t max_iter, double* rank,
+                       uint64_t rank_len, uint64_t* iters, const gtc_options* opt,
+                       gtc_result* result) {
+    return guarded([&] {
+        GTC_REQUIRE(b, GTC_ERR_ARG, "batch is NULL");
+        const uint32_t n = b->u->n, m = b->u->m;
+        GTC_REQUIRE(!weight || weight_len >= m, GTC_ERR_ARG, "weight map is shorter than the edge bound");
+        GTC_REQUIRE(rank || n == 0, GTC_ERR_ARG, "rank is NULL");
+        GTC_REQUIRE(rank_len >= n, GTC_ERR_ARG, "rank map is shorter than the vertex bound");
+        cudaStream_t s = stream_of(b->u, opt);
+        // staging buffers live with the batch, so the captured solve is replayed
+        if (weight && b->wstage.n < m) b->wstage.alloc(m, b->u->home);
+        if (b->rstage.n < n || !b->rstage.get()) b->rstage.alloc(n, b->u->home);
+        GTC_CUDA(cudaStreamSynchronize(b->u->home));
+        if (weight && m)
+            GTC_CUDA(cudaMemcpyAsync(b->wstage.get(), weight, (size_t)m * 8, cudaMemcpyHostToDevice, s));
+        gtc_dvec vw{weight ? b->wstage.get() : nullptr, m, GTC_F64, 0};
+        gtc_dvec vr{b->rstage.get(), n, GTC_F64, 0};
+        gtc_options o = opt ? *opt : gtc_options{};
+        o.stream = (void*)s;
+        const int st = gtc_pagerank_batch_device(b, weight ? &vw : nullptr, damping, epsilon,
+                                                 max_iter, &vr, iters, &o, result);
+        if (st != GTC_OK) throw Error{st, gtc_last_error()};
+        if (n) GTC_CUDA(cudaMemcpyAsync(rank, b->rstage.get(), (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
 }  // extern "C"

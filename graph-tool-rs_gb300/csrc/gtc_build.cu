@@ -437,7 +437,12 @@ static void relabel_half(uint32_t n, uint32_t m, const uint32_t* perm, const uin
     h = std::move(nh);
 }
 
-void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt) {
+__global__ void k_iota(uint32_t n, uint32_t* __restrict__ a, uint32_t* __restrict__ b) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = b[i] = (uint32_t)i;
+}
+
+void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt, bool relabel) {
     cudaStream_t s = g->home;
     const uint32_t n = g->n, m = g->m;
     const unsigned TB = 256;
@@ -497,10 +502,15 @@ void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt) {
         L += 2;
     }
 
-    // relabel by descending out-degree (stable: ties keep index order)
+    // relabel by descending out-degree (stable: ties keep index order); a
+    // packed batch of graphs keeps its labels (each graph stays contiguous)
     g->perm.alloc(n, s);
     g->iperm.alloc(n, s);
-    if (n) {
+    if (n && !relabel) {
+        k_iota<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->perm.get(), g->iperm.get());
+        GTC_LAUNCHED();
+        L += 1;
+    } else if (n) {
         DevBuf<uint32_t> deg(n, s), key(n, s), skey(n, s);
         DevBuf<unsigned> mx(1, s);
         GTC_CUDA(cudaMemsetAsync(mx.get(), 0, sizeof(unsigned), s));

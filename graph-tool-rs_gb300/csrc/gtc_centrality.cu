@@ -780,10 +780,11 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         A.out = dq;
         A.x = yc, A.prev = rc, A.next = rn, A.ynext = yn;
         const int var = tuned_variant<MODE_PAGERANK>(*U, A, W, s, &L);
-        // the segmented sweep (gtc_seg.cu), where the view allows it and it
-        // measures faster than the pull sweep on this graph
+        // the segmented sweep (gtc_seg.cu) is opt-in (GTC_SWEEP_VARIANT=2): on
+        // the R-MAT graphs measured so far it is slower than the pull sweep
         SegPlan* SP = nullptr;
-        if (seg_supported(view)) {
+        const char* pin = std::getenv("GTC_SWEEP_VARIANT");
+        if (pin && std::atoi(pin) == 2 && seg_supported(view)) {
             SegPlan& sp = g->seg[view.reversed ? 1 : 0];
             if (!sp.built) build_seg(g, view, s, sp);
             SP = &sp;
@@ -792,55 +793,27 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         DevBuf<double> spart;
         DevBuf<unsigned> sticket;
         SegArgs SA{};
-        bool use_seg = false;
-        if (SP) {
-            int& ch = SP->choice[W ? 1 : 0];
-            if (const char* e = std::getenv("GTC_SWEEP_VARIANT")) ch = std::atoi(e) == 2 ? 1 : 0;
-            if (ch != 0) {
-                if (W) {
-                    wseg.alloc(SP->m, s);
-                    seg_gather_weights(*SP, in.weight, wseg.get(), s);
-                    L++;
-                }
-                spart.alloc(seg_part_slots(*SP), s);
-                sticket.alloc(1, s);
-                GTC_CUDA(cudaMemsetAsync(sticket.get(), 0, sizeof(unsigned), s));
-                SA.ws = wseg.get();
-                SA.pers = pers32.get();
-                SA.uniform = (float)P.uniform;
-                SA.one_minus_d = (float)(1.0 - d);
-                SA.d = (float)d;
-                SA.psink = dq + 1;
-                SA.invdeg = invdeg.get();
-                SA.sink = P.sink.get();
-                SA.part = spart.get();
-                SA.ticket = sticket.get();
-                SA.out = dq;
-                SA.y = yc, SA.prev = rc, SA.next = rn, SA.ynext = yn;
-                if (ch < 0) {  // time both, the first round warming caches up
-                    cudaEvent_t e0, e1;
-                    GTC_CUDA(cudaEventCreate(&e0));
-                    GTC_CUDA(cudaEventCreate(&e1));
-                    float t_seg = 0.f, t_pull = 0.f;
-                    for (int rep = 0; rep < 2; ++rep) {
-                        GTC_CUDA(cudaEventRecord(e0, s));
-                        seg_sweep(*SP, SA, W, s);
-                        GTC_CUDA(cudaEventRecord(e1, s));
-                        GTC_CUDA(cudaEventSynchronize(e1));
-                        GTC_CUDA(cudaEventElapsedTime(&t_seg, e0, e1));
-                        GTC_CUDA(cudaEventRecord(e0, s));
-                        launch_sweep<MODE_PAGERANK>(var, A, W, s);
-                        GTC_CUDA(cudaEventRecord(e1, s));
-                        GTC_CUDA(cudaEventSynchronize(e1));
-                        GTC_CUDA(cudaEventElapsedTime(&t_pull, e0, e1));
-                        L += 3;
-                    }
-                    cudaEventDestroy(e0);
-                    cudaEventDestroy(e1);
-                    ch = t_seg < t_pull ? 1 : 0;
-                }
-                use_seg = ch == 1;
+        const bool use_seg = SP != nullptr;
+        if (use_seg) {
+            if (W) {
+                wseg.alloc(SP->m, s);
+                seg_gather_weights(*SP, in.weight, wseg.get(), s);
+                L++;
             }
+            spart.alloc(seg_part_slots(*SP), s);
+            sticket.alloc(1, s);
+            GTC_CUDA(cudaMemsetAsync(sticket.get(), 0, sizeof(unsigned), s));
+            SA.ws = wseg.get();
+            SA.pers = pers32.get();
+            SA.uniform = (float)P.uniform;
+            SA.one_minus_d = (float)(1.0 - d);
+            SA.d = (float)d;
+            SA.psink = dq + 1;
+            SA.invdeg = invdeg.get();
+            SA.sink = P.sink.get();
+            SA.part = spart.get();
+            SA.ticket = sticket.get();
+            SA.out = dq;
         }
         // a tuning trial wrote the dangling mass of its output: restore it
         GTC_CUDA(cudaMemcpyAsync(dq + 1, dp + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));

@@ -146,7 +146,6 @@ struct SegPlan {
     DevBuf<uint16_t> pdest;           // per pair (group order): local destination | run start << 15
     DevBuf<uint32_t> gpair;           // per destination group: first pair (ngroups + 1)
     DevBuf<float> partial;            // per pair: the sweep's pair sums (scratch)
-    int choice[2] = {-1, -1};         // tuned per [weighted]: 1 = the segmented sweep is faster
     bool built = false;
 };
 
@@ -176,6 +175,41 @@ struct SegArgs {
 
 }  // namespace gtc
 
+namespace gtc {
+// What a captured batch solve depends on besides the graph (gtc_batch.cu).
+struct BatchKey {
+    const void* w = nullptr;
+    int wdt = -1;
+    void* out = nullptr;
+    int odt = -1;
+    double d = 0.0, eps = 0.0;
+    uint64_t max_iter = 0;
+    bool operator==(const BatchKey& o) const {
+        return w == o.w && wdt == o.wdt && out == o.out && odt == o.odt && d == o.d &&
+               eps == o.eps && max_iter == o.max_iter;
+    }
+};
+}  // namespace gtc
+
+struct gtc_graph;
+
+// Many graphs packed as one block-diagonal graph (gtc_batch.cu): graph k owns
+// vertices [voff[k], voff[k+1]) of the union `u`, whose labels are kept.
+struct gtc_graph_batch {
+    gtc_graph* u = nullptr;
+    uint32_t G = 0;
+    std::vector<uint32_t> hvoff, heoff;      // host copies, G + 1 each
+    gtc::DevBuf<uint32_t> voff, order;       // order: graphs by descending edge count
+    gtc::DevBuf<float> invdeg, r0, r1, y0, y1, wout, wpull;
+    gtc::DevBuf<uint8_t> sink;
+    gtc::DevBuf<uint64_t> iters;
+    gtc::DevBuf<unsigned> counter;
+    gtc::DevBuf<double> wstage, rstage;      // host-API staging
+    cudaGraphExec_t exec = nullptr;          // the captured solve
+    gtc::BatchKey key{};
+    uint64_t launches_per_solve = 0;
+};
+
 struct gtc_graph {
     gtc_graph() = default;
     gtc_graph(uint32_t n_, uint32_t m_) : n(n_), m(m_) {}
@@ -201,7 +235,7 @@ struct gtc_graph {
 namespace gtc {
 
 // graph build (gtc_build.cu)
-void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt);
+void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt, bool relabel = true);
 void build_schedule(gtc_graph* g, bool in_dir, uint32_t cap);
 
 // A device vector of either float type.
@@ -236,6 +270,11 @@ __device__ __forceinline__ double ld_any(const void* p, int dtype, size_t i) {
 __device__ __forceinline__ float ld_f32(const void* p, int dtype, size_t i) {
     return dtype == GTC_F64 ? (float)((const double*)p)[i] : ((const float*)p)[i];
 }
+
+// batches of graphs (gtc_batch.cu)
+void pagerank_batch(gtc_graph_batch* b, const DVec& weight, double damping, double epsilon,
+                    uint64_t max_iter, void* out, int out_dtype, uint64_t* iters, bool timing,
+                    gtc_result* res, cudaStream_t s);
 
 // segmented pull sweep (gtc_seg.cu)
 struct View;

@@ -9,6 +9,6 @@ on one NVIDIA GB300, behind the reference's Python module surface.
     from graph_tool.centrality import pagerank
     rank = pagerank(g)                        # graph-tool's signature
 """
-from ._rust import Graph, PropertyMap, value_types  # noqa: F401
+from ._rust import Graph, GraphBatch, PropertyMap, value_types  # noqa: F401
 
-__all__ = ["Graph", "PropertyMap", "value_types"]
+__all__ = ["Graph", "GraphBatch", "PropertyMap", "value_types"]

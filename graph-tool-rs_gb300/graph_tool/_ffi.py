@@ -104,6 +104,16 @@ SIGNATURES = {
                                        u64p, u32p, f64p, C.c_double, C.POINTER(PowerIteration),
                                        C.POINTER(DVec), u64p, C.POINTER(Options),
                                        C.POINTER(Result)]),
+    "gtc_graph_batch_create": (C.c_int, [C.c_uint64, u64p, u64p, u32p, u32p,
+                                         C.POINTER(C.c_void_p)]),
+    "gtc_graph_batch_destroy": (C.c_int, [C.c_void_p]),
+    "gtc_graph_batch_info": (C.c_int, [C.c_void_p, u64p, u64p, u64p]),
+    "gtc_pagerank_batch": (C.c_int, [C.c_void_p, f64p, C.c_uint64, C.c_double, C.c_double,
+                                     C.c_uint64, f64p, C.c_uint64, u64p, C.POINTER(Options),
+                                     C.POINTER(Result)]),
+    "gtc_pagerank_batch_device": (C.c_int, [C.c_void_p, C.POINTER(DVec), C.c_double, C.c_double,
+                                            C.c_uint64, C.POINTER(DVec), u64p, C.POINTER(Options),
+                                            C.POINTER(Result)]),
     "gtc_pagerank_adjoint": (C.c_int, [C.c_void_p, C.POINTER(View), f64p, C.c_uint64, f64p,
                                        C.c_uint64, C.c_double, C.POINTER(PowerIteration), f64p,
                                        f64p, f64p, f64p, C.POINTER(Options), C.POINTER(Result)]),

@@ -282,6 +282,69 @@ class Graph:
         return ranks, iters
 
 
+class GraphBatch:
+    """Many graphs of uneven sizes, packed as one block-diagonal graph and
+    solved together (no counterpart in the reference, which takes one graph
+    per call).  ``graphs`` is a sequence of (n, src, tgt) with local vertex
+    indices; the edges of each graph are added in array order."""
+
+    def __init__(self, graphs):
+        G = len(graphs)
+        if G == 0:
+            raise ValueError("a batch holds at least one graph")
+        self._n = np.array([int(g[0]) for g in graphs], np.uint64)
+        self._m = np.array([len(g[1]) for g in graphs], np.uint64)
+        voff = np.zeros(G + 1, np.uint64)
+        eoff = np.zeros(G + 1, np.uint64)
+        voff[1:] = np.cumsum(self._n)
+        eoff[1:] = np.cumsum(self._m)
+        src = np.ascontiguousarray(np.concatenate([np.asarray(g[1], np.int64) for g in graphs])
+                                   if eoff[-1] else np.zeros(0), dtype=np.uint32)
+        tgt = np.ascontiguousarray(np.concatenate([np.asarray(g[2], np.int64) for g in graphs])
+                                   if eoff[-1] else np.zeros(0), dtype=np.uint32)
+        h = C.c_void_p()
+        _ffi.check(_ffi.lib().gtc_graph_batch_create(G, _ffi.ptr(voff, _ffi.u64p),
+                                                     _ffi.ptr(eoff, _ffi.u64p),
+                                                     _ffi.ptr(src, _ffi.u32p),
+                                                     _ffi.ptr(tgt, _ffi.u32p), C.byref(h)))
+        self._h = h.value
+        self.voff, self.eoff = voff, eoff
+
+    def __len__(self):
+        return len(self._n)
+
+    def handle(self):
+        return self._h
+
+    def pagerank(self, weight=None, damping: float = 0.85, epsilon: float = 1e-6,
+                 max_iter: int = 0, result: bool = False):
+        """pagerank (centrality.rs:234-248) of every graph; ``weight`` per edge
+        of the packed edge list.  Returns (ranks, iters): ranks per vertex of
+        the packed vertex list (graph k is ranks[voff[k]:voff[k+1]])."""
+        n, m = int(self.voff[-1]), int(self.eoff[-1])
+        w = None
+        if weight is not None:
+            w = np.ascontiguousarray(weight, dtype=np.float64)
+            if w.size < m:
+                raise ValueError(f"weight holds {w.size} entries, the batch has {m} edges")
+        ranks = np.zeros(max(n, 1), np.float64)
+        iters = np.zeros(len(self), np.uint64)
+        res = _ffi.Result()
+        opt = _ffi.Options(_ffi.GTC_PREC_F32, 0, None, 0, 0)
+        _ffi.check(_ffi.lib().gtc_pagerank_batch(
+            self._h, _ffi.ptr(w, _ffi.f64p), 0 if w is None else w.size, float(damping),
+            float(epsilon), int(max_iter or 0), _ffi.ptr(ranks, _ffi.f64p), n,
+            _ffi.ptr(iters, _ffi.u64p), C.byref(opt), C.byref(res)))
+        out = (ranks[:n], iters)
+        return out + (res,) if result else out
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _ffi._lib is not None:
+            _ffi.lib().gtc_graph_batch_destroy(h)
+            self._h = None
+
+
 _PRECISIONS = {"f32": _ffi.GTC_PREC_F32, "f64_exact": _ffi.GTC_PREC_F64_EXACT}
 
 

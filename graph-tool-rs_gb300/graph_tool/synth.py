@@ -151,3 +151,35 @@ def rmat_cpu(scale: int, edge_factor: int = 16, abcd=(0.57, 0.19, 0.19, 0.05),
         first.sort()
         src, tgt = src[first], tgt[first]
     return n, src.astype(np.uint32), tgt.astype(np.uint32)
+
+
+def sbm_batch(G: int, n_min: int = 100, n_max: int = 100_000, blocks: int = 4,
+              k_in: float = 16.0, k_out: float = 2.0, seed: int = 3):
+    """G directed stochastic-block-model graphs of log-uniform sizes in
+    [n_min, n_max]: ``blocks`` equal blocks, edge probability k_in / n inside
+    a block and k_out / n across (mean out-degree (k_in + (blocks - 1) k_out)
+    / blocks).  Each block pair draws its edge count (binomial) and then its
+    endpoints uniformly; duplicates and self-loops are dropped (first draw
+    kept).  Returns a list of (n, src, tgt) with local indices."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(G):
+        n = int(round(np.exp(rng.uniform(np.log(n_min), np.log(n_max)))))
+        bounds = np.linspace(0, n, blocks + 1).round().astype(np.int64)
+        srcs, tgts = [], []
+        for a in range(blocks):
+            for b in range(blocks):
+                na, nb = bounds[a + 1] - bounds[a], bounds[b + 1] - bounds[b]
+                p = (k_in if a == b else k_out) / n
+                cnt = rng.binomial(int(na * nb), min(p, 1.0)) if na and nb else 0
+                srcs.append(bounds[a] + rng.integers(0, max(na, 1), cnt))
+                tgts.append(bounds[b] + rng.integers(0, max(nb, 1), cnt))
+        s = np.concatenate(srcs) if srcs else np.zeros(0, np.int64)
+        t = np.concatenate(tgts) if tgts else np.zeros(0, np.int64)
+        keep = s != t
+        s, t = s[keep], t[keep]
+        key = s * n + t
+        _, first = np.unique(key, return_index=True)
+        first.sort()
+        out.append((n, s[first].astype(np.uint32), t[first].astype(np.uint32)))
+    return out

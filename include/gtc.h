@@ -232,6 +232,43 @@ int gtc_ppr_batch_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* wei
                          const gtc_power_iteration* params, gtc_dvec* ranks, uint64_t* iters,
                          const gtc_options* opt, gtc_result* result);
 
+/* ---- many graphs in one call --------------------------------------------
+ *
+ * G graphs packed as one block-diagonal graph (no counterpart in the
+ * reference, which solves one graph per call): graph k has n_k = voff[k+1] -
+ * voff[k] vertices and the edges eoff[k] .. eoff[k+1]-1 of src/tgt, whose
+ * endpoints are LOCAL indices (0 .. n_k - 1), added in array order as
+ * add_edge calls of that graph (crates/gt-core/src/adj/list.rs:299-321).
+ * voff[0] = eoff[0] = 0; voff[G] and eoff[G] are the totals (< 2^32).
+ * Host arrays. */
+typedef struct gtc_graph_batch gtc_graph_batch;
+
+int gtc_graph_batch_create(uint64_t G, const uint64_t* voff, const uint64_t* eoff,
+                           const uint32_t* src, const uint32_t* tgt, gtc_graph_batch** out);
+int gtc_graph_batch_destroy(gtc_graph_batch* b);
+int gtc_graph_batch_info(const gtc_graph_batch* b, uint64_t* graphs, uint64_t* vertices,
+                         uint64_t* edges);
+
+/* pagerank (centrality.rs:234-248) of every graph of the batch: uniform
+ * personalisation 1/n_k, each graph with its own dangling mass, L1 change and
+ * stop (the first sweep whose change is below epsilon, or max_iter; 0 =
+ * uncapped).  weight: per edge of the packed edge list (NULL = Unity);
+ * rank: per vertex of the packed vertex list (out, fresh start); iters[k]:
+ * sweeps of graph k.  GTC_PREC_F32.  One persistent kernel solves all graphs
+ * (a CTA per graph at a time, largest first); the launches of a solve are
+ * captured into a CUDA graph and replayed while the arrays keep their
+ * addresses.  Host arrays. */
+int gtc_pagerank_batch(gtc_graph_batch* b, const double* weight, uint64_t weight_len,
+                       double damping, double epsilon, uint64_t max_iter, double* rank,
+                       uint64_t rank_len, uint64_t* iters, const gtc_options* opt,
+                       gtc_result* result);
+
+/* As gtc_pagerank_batch with weight and rank in device memory (FP32 or
+ * FP64); iters stays a host array. */
+int gtc_pagerank_batch_device(gtc_graph_batch* b, const gtc_dvec* weight, double damping,
+                              double epsilon, uint64_t max_iter, gtc_dvec* rank, uint64_t* iters,
+                              const gtc_options* opt, gtc_result* result);
+
 /* ---- gradients ---------------------------------------------------------
  *
  * The adjoint of PageRank (no counterpart in the reference, which has no

@@ -69,3 +69,15 @@ def test_synth_generators_are_deterministic(gtc):
     assert len(set(zip(src.tolist(), tgt.tolist()))) == src.size  # no duplicates
     n, s, t = synth.rmat_cpu(10)
     assert len(set(zip(s.tolist(), t.tolist()))) == s.size
+
+
+def test_graph_batch_rejects_bad_input(gtc):
+    """The batch's inputs are checked before any device work: endpoints
+    beyond their own graph, decreasing offsets, an empty batch."""
+    import pytest as _pt
+    with _pt.raises(ValueError):
+        gtc.GraphBatch([(3, [0, 3], [1, 2])])          # 3 is not a vertex of a 3-vertex graph
+    with _pt.raises(ValueError):
+        gtc.GraphBatch([(2, [0], [1]), (2, [0], [5])])  # local indices: 5 >= 2
+    with _pt.raises(ValueError):
+        gtc.GraphBatch([])
