@@ -519,6 +519,7 @@ int gtc_ppr_batch(gtc_graph* g, const gtc_view* view, const double* weight, uint
 static void destroy_batch(gtc_graph_batch* b) {
     if (!b) return;
     if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->side) cudaStreamDestroy(b->side);
     gtc_graph* u = b->u;
     b->u = nullptr;
     delete b;  // its buffers are freed on the union's home stream
@@ -538,8 +539,8 @@ int gtc_graph_batch_create(uint64_t G, const uint64_t* voff, const uint64_t* eof
                         "voff/eoff must not decrease");
         }
         const uint64_t n = voff[G], m = eoff[G];
-        GTC_REQUIRE(n <= 0xFFFFFFFEull && m <= 0xFFFFFFFEull, GTC_ERR_ARG,
-                    "the packed batch exceeds the index space (MAX_INDEX = 2^32 - 2)");
+        GTC_REQUIRE(n <= 0xFFFFF000ull && m <= 0xFFFFFFFEull, GTC_ERR_ARG,
+                    "the packed batch exceeds the index space (n <= 2^32 - 4096, m <= 2^32 - 2)");
         GTC_REQUIRE(m == 0 || (src && tgt), GTC_ERR_ARG, "src/tgt is NULL");
         // endpoints to packed labels, checked against their own graph
         std::vector<uint32_t> gs(m), gt(m);
@@ -557,26 +558,45 @@ int gtc_graph_batch_create(uint64_t G, const uint64_t* voff, const uint64_t* eof
             b->u = new_graph(n, m);
             b->G = (uint32_t)G;
             cudaStream_t h = b->u->home;
+            b->hvoff.resize(G + 1);
+            b->heoff.resize(G + 1);
+            for (uint64_t k = 0; k <= G; ++k) b->hvoff[k] = (uint32_t)voff[k], b->heoff[k] = (uint32_t)eoff[k];
+            b->voff.alloc(G + 1, h);
+            GTC_CUDA(cudaMemcpyAsync(b->voff.get(), b->hvoff.data(), (G + 1) * 4, cudaMemcpyHostToDevice, h));
             {
                 DevBuf<uint32_t> ds(m, h), dt(m, h);
                 if (m) {
                     GTC_CUDA(cudaMemcpyAsync(ds.get(), gs.data(), m * 4, cudaMemcpyHostToDevice, h));
                     GTC_CUDA(cudaMemcpyAsync(dt.get(), gt.data(), m * 4, cudaMemcpyHostToDevice, h));
                 }
-                build_halves(b->u, ds.get(), dt.get(), /*relabel=*/false);
+                batch_layout(b, ds.get(), dt.get(), h);
             }
-            b->hvoff.resize(G + 1);
-            b->heoff.resize(G + 1);
-            for (uint64_t k = 0; k <= G; ++k) b->hvoff[k] = (uint32_t)voff[k], b->heoff[k] = (uint32_t)eoff[k];
             std::vector<uint32_t> order(G);
             for (uint32_t k = 0; k < G; ++k) order[k] = k;
             std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c) {
                 return (eoff[a + 1] - eoff[a]) + (voff[a + 1] - voff[a]) >
                        (eoff[c + 1] - eoff[c]) + (voff[c + 1] - voff[c]);
             });
-            b->voff.alloc(G + 1, h);
+            // three queues, in this order: graphs for a cluster pair (up to
+            // 2 * GB_CL_CAP vertices), for one CTA (up to GB_CL_CAP), and the
+            // larger ones, gathered from global memory
+            auto queue = [&](uint32_t k) {
+                const uint64_t nk = voff[k + 1] - voff[k];
+                return nk <= GB_CL_CAP ? 1 : (nk + 1) / 2 <= GB_CL_CAP ? 0 : 2;
+            };
+            std::stable_sort(order.begin(), order.end(),
+                             [&](uint32_t a, uint32_t c) { return queue(a) < queue(c); });
+            b->n_pair = b->n_single = b->n_global = 0;
+            b->smem_floats = 0;
+            for (uint32_t k : order) {
+                const uint32_t nk = (uint32_t)(voff[k + 1] - voff[k]);
+                switch (queue(k)) {
+                    case 0: ++b->n_pair, b->smem_floats = std::max(b->smem_floats, (nk + 1) / 2); break;
+                    case 1: ++b->n_single, b->smem_floats = std::max(b->smem_floats, nk); break;
+                    default: ++b->n_global;
+                }
+            }
             b->order.alloc(G, h);
-            GTC_CUDA(cudaMemcpyAsync(b->voff.get(), b->hvoff.data(), (G + 1) * 4, cudaMemcpyHostToDevice, h));
             GTC_CUDA(cudaMemcpyAsync(b->order.get(), order.data(), G * 4, cudaMemcpyHostToDevice, h));
             GTC_CUDA(cudaStreamSynchronize(h));
         } catch (...) {
@@ -606,6 +626,8 @@ int gtc_pagerank_batch_device(gtc_graph_batch* b, const gtc_dvec* weight, double
                               const gtc_options* opt, gtc_result* result) {
     return guarded([&] {
         GTC_REQUIRE(b, GTC_ERR_ARG, "batch is NULL");
+        GTC_REQUIRE(max_iter > 0 || epsilon > 0, GTC_ERR_ARG,
+                    "epsilon must be positive when max_iter is 0 (the solve would never stop)");
         GTC_REQUIRE(!std::isnan(damping) && !std::isnan(epsilon), GTC_ERR_ARG,
                     "damping or epsilon is NaN");
         GTC_REQUIRE(!opt || opt->precision == GTC_PREC_F32, GTC_ERR_ARG,

@@ -124,16 +124,17 @@ __global__ void k_degree_f32(uint32_t n, const uint32_t* __restrict__ push_off,
     const uint32_t sub = threadIdx.x & 7;
     const size_t v = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
     const bool in = v < n;  // whole groups leave together: the shuffles stay full-warp
-    Kahan k;
+    KahanBlocked kb;
     if (in) {
         const uint32_t b = push_off[v], e = push_off[v + 1];
         uint32_t p = b + sub;
         for (; p + 24 < e; p += 32) {  // four loads in flight
             const float x0 = wout[p], x1 = wout[p + 8], x2 = wout[p + 16], x3 = wout[p + 24];
-            k.add(x0), k.add(x1), k.add(x2), k.add(x3);
+            kb.add(x0), kb.add(x1), kb.add(x2), kb.add(x3);
         }
-        for (; p < e; p += 8) k.add(wout[p]);
+        for (; p < e; p += 8) kb.add(wout[p]);
     }
+    Kahan k = kb.fold();
     group8_merge_kahan(k);
     if (in && sub == 0) {
         const double kd = (double)k.s + (double)k.c;

@@ -195,12 +195,42 @@ struct gtc_graph;
 
 // Many graphs packed as one block-diagonal graph (gtc_batch.cu): graph k owns
 // vertices [voff[k], voff[k+1]) of the union `u`, whose labels are kept.
+namespace gtc {
+// Most vertices whose gathered vector (4 bytes each) one CTA of the batch
+// kernels holds in shared memory: a graph of up to GB_CL_CAP vertices is
+// solved by one CTA, one of up to 2 * GB_CL_CAP by a cluster of two.
+constexpr uint32_t GB_CL_CAP = 57344;
+// Longest row kept in the batch's 32-row slices; longer rows are summed by a
+// whole warp.
+constexpr uint32_t GB_SL_CAP = 128;
+// The batch's rows are ordered by in-degree only inside windows of this many
+// consecutive labels of their graph, which keeps the input's locality.
+constexpr uint32_t GB_WIN = 1024;
+}  // namespace gtc
+
 struct gtc_graph_batch {
     gtc_graph* u = nullptr;
     uint32_t G = 0;
     std::vector<uint32_t> hvoff, heoff;      // host copies, G + 1 each
-    gtc::DevBuf<uint32_t> voff, order;       // order: graphs by descending edge count
-    gtc::DevBuf<float> invdeg, r0, r1, y0, y1, wout, wpull;
+    // order: the n_pair graphs of GB_CL_CAP + 1 .. 2 * GB_CL_CAP vertices,
+    // the n_single of at most GB_CL_CAP, then the n_global larger ones; each
+    // queue by descending edges + vertices
+    gtc::DevBuf<uint32_t> voff, order;
+    // Layout (batch_layout, gtc_batch.cu).  Inside each graph the vertices
+    // are relabelled: rows of more than GB_SL_CAP in-edges first, the others
+    // by descending in-degree inside windows of GB_WIN labels; vperm[new] =
+    // packed label.  A graph's first glong[g] rows keep their pull entries
+    // in CSR order from gebase[g]; the others form slices of 32 rows, gsl[g]
+    // .. gsl[g+1]-1, each stored column-major from sl_off[s] (entry j of lane
+    // i at sl_off[s] + 32*j + i; short lanes padded).
+    gtc::DevBuf<uint32_t> vperm, glong, gsl, gebase, sl_off;
+    gtc::DevBuf<uint32_t> eidx, eeid;         // layout entries: source, edge id (pads ~0u)
+    gtc::DevBuf<float> wlay;                  // weights in layout order
+    uint64_t n_lay = 0;
+    uint32_t n_pair = 0, n_single = 0, n_global = 0;
+    uint32_t smem_floats = 0;                // x entries a CTA of the first two queues holds
+    cudaStream_t side = nullptr;             // the global queue's stream while captured
+    gtc::DevBuf<float> invdeg, r0, r1, y0, y1, wout;
     gtc::DevBuf<uint8_t> sink;
     gtc::DevBuf<uint64_t> iters;
     gtc::DevBuf<unsigned> counter;
@@ -272,6 +302,7 @@ __device__ __forceinline__ float ld_f32(const void* p, int dtype, size_t i) {
 }
 
 // batches of graphs (gtc_batch.cu)
+void batch_layout(gtc_graph_batch* b, uint32_t* d_src, uint32_t* d_tgt, cudaStream_t s);
 void pagerank_batch(gtc_graph_batch* b, const DVec& weight, double damping, double epsilon,
                     uint64_t max_iter, void* out, int out_dtype, uint64_t* iters, bool timing,
                     gtc_result* res, cudaStream_t s);
@@ -363,6 +394,32 @@ struct Kahan {
         c = __fadd_rn(c, __fadd_rn(oc, e));
     }
     __device__ __forceinline__ float value() const { return __fadd_rn(s, c); }
+};
+
+// Compensated sum of a long run of terms.  One (s, c) pair over many terms
+// of similar size collects a systematic rounding error in c, and c, itself
+// summed plainly, then loses about (terms x ulp(c)): 114,687 equal terms of
+// 4.7e-6 lose 4e-7 of their 0.54.  Merging the pair of every block of
+// KB_BLOCK terms into an outer pair keeps c small.  Up to KB_BLOCK terms the
+// result is the single pair's, bit for bit.
+constexpr uint32_t KB_BLOCK = 256;
+
+struct KahanBlocked {
+    Kahan outer, inner;
+    uint32_t k = 0;
+    __device__ __forceinline__ void add(float x) {
+        inner.add(x);
+        if (++k == KB_BLOCK) {
+            outer.merge(inner.s, inner.c);
+            inner = Kahan();
+            k = 0;
+        }
+    }
+    __device__ __forceinline__ Kahan fold() const {
+        Kahan r = outer;
+        r.merge(inner.s, inner.c);
+        return r;
+    }
 };
 
 __device__ __forceinline__ void warp_merge_kahan(Kahan& k) {

@@ -126,9 +126,10 @@ __global__ void __launch_bounds__(NA_NT) k_na_sweep(NaArgs A) {
     const float psink = (float)*A.psink;
     Kahan da, sa;
     for (uint32_t v = gw; v < A.n; v += nw) {
-        Kahan k;
+        KahanBlocked kb;
         for (uint32_t p = A.off[v] + lane, e = A.off[v + 1]; p < e; p += 32)
-            k.add(A.yprev[A.src[p]]);
+            kb.add(A.yprev[A.src[p]]);
+        Kahan k = kb.fold();
         warp_merge_kahan(k);
         if (lane == 0) {
             const float r = __fadd_rn(__fmul_rn(psink, A.uniform), k.value());

@@ -239,7 +239,8 @@ int gtc_ppr_batch_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* wei
  * voff[k] vertices and the edges eoff[k] .. eoff[k+1]-1 of src/tgt, whose
  * endpoints are LOCAL indices (0 .. n_k - 1), added in array order as
  * add_edge calls of that graph (crates/gt-core/src/adj/list.rs:299-321).
- * voff[0] = eoff[0] = 0; voff[G] and eoff[G] are the totals (< 2^32).
+ * voff[0] = eoff[0] = 0; voff[G] and eoff[G] are the totals (voff[G] <=
+ * 2^32 - 4096, eoff[G] <= 2^32 - 2).
  * Host arrays. */
 typedef struct gtc_graph_batch gtc_graph_batch;
 
@@ -254,10 +255,15 @@ int gtc_graph_batch_info(const gtc_graph_batch* b, uint64_t* graphs, uint64_t* v
  * stop (the first sweep whose change is below epsilon, or max_iter; 0 =
  * uncapped).  weight: per edge of the packed edge list (NULL = Unity);
  * rank: per vertex of the packed vertex list (out, fresh start); iters[k]:
- * sweeps of graph k.  GTC_PREC_F32.  One persistent kernel solves all graphs
- * (a CTA per graph at a time, largest first); the launches of a solve are
- * captured into a CUDA graph and replayed while the arrays keep their
- * addresses.  Host arrays. */
+ * sweeps of graph k.  GTC_PREC_F32.  Persistent kernels solve all graphs,
+ * largest first: a cluster of two CTAs per graph of up to 114,688 vertices
+ * (its gathered vector in shared memory), one CTA per larger graph; the
+ * launches of a solve are captured into a CUDA graph and replayed while the
+ * arrays keep their addresses.  The device loop is bounded: max_iter 0 with
+ * epsilon <= 0 is GTC_ERR_ARG; a graph whose L1 change is not finite stops
+ * at once (GTC_ERR_ARG after the call); an uncapped graph still running
+ * after 100,000 sweeps stops there (GTC_ERR_TIMEOUT).  In both error cases
+ * rank and iters are still written.  Host arrays. */
 int gtc_pagerank_batch(gtc_graph_batch* b, const double* weight, uint64_t weight_len,
                        double damping, double epsilon, uint64_t max_iter, double* rank,
                        uint64_t rank_len, uint64_t* iters, const gtc_options* opt,

@@ -69,3 +69,26 @@ def test_batch_max_iter(oracle, gtc, graphs):
         want, it = og.pagerank(epsilon=1e-14, max_iter=4, grain=4096)
         got = ranks[b.voff[k]:b.voff[k + 1]]
         assert np.abs(got - want).sum() / np.abs(want).sum() < 1e-6
+
+
+def test_batch_with_graphs_beyond_the_cluster_kernel(oracle, gtc):
+    """Graphs of more than 2 * 57344 vertices run on the single-CTA kernel
+    beside the cluster kernel; both queues in one call, weighted."""
+    from graph_tool import synth
+    rng = np.random.default_rng(13)
+    gs = synth.sbm_batch(6, 100, 3000, seed=12)
+    for n in (120_000, 131_072):
+        m = 3 * n
+        src = rng.integers(0, n, m)
+        tgt = rng.integers(0, n, m)
+        keep = (src != tgt) & ~np.isin(src, rng.choice(n, n // 20, replace=False))
+        gs.insert(2, (n, src[keep].astype(np.uint32), tgt[keep].astype(np.uint32)))
+    gs.append((114_689, np.zeros(0, np.uint32), np.zeros(0, np.uint32)))  # just past the cap
+    gs.append((114_688, np.arange(1, 114_688, dtype=np.uint32), np.zeros(114_687, np.uint32)))
+    b = gtc.GraphBatch(gs)
+    w = rng.uniform(0.1, 1.0, int(b.eoff[-1]))
+    # epsilon 1e-6: an FP32 iterate whose every entry moves by one ulp
+    # changes by about 2^-23 ~ 1.2e-7 in L1, so 1e-7 can sit at the floor
+    ranks, iters = b.pagerank(weight=w, epsilon=1e-6, max_iter=1000)
+    worst = _check(oracle, gs, ranks, iters, b.voff, w, b.eoff, eps=1e-6)
+    print(f"graph batch with large graphs: worst rel L1 {worst:.2e}")

@@ -81,3 +81,16 @@ def test_graph_batch_rejects_bad_input(gtc):
         gtc.GraphBatch([(2, [0], [1]), (2, [0], [5])])  # local indices: 5 >= 2
     with _pt.raises(ValueError):
         gtc.GraphBatch([])
+
+
+def test_graph_batch_uncapped_needs_positive_epsilon(gtc):
+    """max_iter 0 with epsilon <= 0 would never stop on the device: refused
+    before any device work."""
+    import ctypes as C
+    from graph_tool import _ffi
+    L = _ffi.lib()
+    r = _ffi.Result()
+    st = L.gtc_pagerank_batch_device(C.c_void_p(1), None, 0.85, 0.0, 0, None, None, None,
+                                     C.byref(r))
+    assert st == _ffi.GTC_ERR_ARG
+    assert b"epsilon" in L.gtc_last_error()
