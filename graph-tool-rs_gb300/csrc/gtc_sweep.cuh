@@ -204,9 +204,10 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
             const float* wp = WEIGHTED ? A.sw + b + lane : nullptr;
             KahanLite acc;
             uint32_t j = 0;
-            for (; j + 4 <= len; j += 4) {
-                const uint32_t s0 = __ldcs(ip), s1 = __ldcs(ip + 32), s2 = __ldcs(ip + 64),
-                               s3 = __ldcs(ip + 96);
+            // four entries a step; the next step's four indices are loaded
+            // before this step's gathers, so an index load and a gather are
+            // in flight together instead of one after the other
+            auto step = [&](uint32_t s0, uint32_t s1, uint32_t s2, uint32_t s3) {
                 float v0, v1, v2, v3;
                 if (H) {
                     v0 = gather<HOT>(A, hot, s0), v1 = gather<HOT>(A, hot, s1);
@@ -226,7 +227,20 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
                 acc.add(v1);
                 acc.add(v2);
                 acc.add(v3);
+            };
+            if (len >= 4) {
+                uint32_t s0 = __ldcs(ip), s1 = __ldcs(ip + 32), s2 = __ldcs(ip + 64),
+                         s3 = __ldcs(ip + 96);
                 ip += 128;
+                for (; j + 8 <= len; j += 4) {
+                    const uint32_t n0 = __ldcs(ip), n1 = __ldcs(ip + 32), n2 = __ldcs(ip + 64),
+                                   n3 = __ldcs(ip + 96);
+                    ip += 128;
+                    step(s0, s1, s2, s3);
+                    s0 = n0, s1 = n1, s2 = n2, s3 = n3;
+                }
+                step(s0, s1, s2, s3);
+                j += 4;
             }
             for (; j < len; ++j) {
                 float v = gather<HOT>(A, hot, __ldcs(ip));
