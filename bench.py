@@ -40,6 +40,10 @@ Two more measurements ride on the same line (skipped with --no-secondary):
             one call solves every graph (a persistent kernel, replayed as a
             CUDA graph); graphs per second and edge-sweeps per second.
 
+``--section adjoint|ppr_batch|graph_batch`` runs one of them alone and prints
+its JSON (``--ppr-scale``, ``--ppr-b``, ``--graphs`` shrink the last two for
+profiling; ``--workload`` picks the adjoint's graph).
+
 ``--impl reference`` times that CPU restatement alone (the reference itself
 is Rust and cannot be built here).  Inputs are larger than L2 (the graph's
 index arrays alone are ~1 GB), so no flush runs between steps.
@@ -427,12 +431,30 @@ def main():
     ap.add_argument("--cpu-sweeps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--section", choices=["adjoint", "ppr_batch", "graph_batch"],
+                    help="run only this secondary measurement (adjoint on --workload's graph) "
+                         "and print its JSON")
+    ap.add_argument("--ppr-scale", type=int, default=22, help="R-MAT scale of the ppr_batch graph")
+    ap.add_argument("--ppr-b", type=int, default=256, help="personalisation vectors of ppr_batch")
+    ap.add_argument("--graphs", type=int, default=4096, help="graphs of graph_batch")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     rank, world, local = env_rank()
 
     import numpy as np
     import torch
+
+    if args.section in ("ppr_batch", "graph_batch"):
+        from graph_tool import _ffi
+        device = torch.device("cuda", local)
+        torch.cuda.set_device(device)
+        stream = torch.cuda.current_stream(device)
+        if args.section == "ppr_batch":
+            out = ppr_section(_ffi.lib(), device, stream, B=args.ppr_b, scale=args.ppr_scale)
+        else:
+            out = graph_batch_section(_ffi.lib(), device, stream, G=args.graphs)
+        print(json.dumps({"section": args.section, **out}), flush=True)
+        return
 
     if world > 1:
         import torch.distributed as dist
@@ -491,6 +513,10 @@ def main():
                                          C.c_void_p(tgt.data_ptr()),
                                          C.c_void_p(stream.cuda_stream), C.byref(h)))
     _ffi.check(L.gtc_graph_set_stream(h, C.c_void_p(stream.cuda_stream)))
+    if args.section == "adjoint":
+        out = adjoint_section(L, h, n, m, device, stream, wl)
+        print(json.dumps({"section": "adjoint", **out}), flush=True)
+        return
     wvec = _ffi.DVec.of(w) if w is not None else None
     params = _ffi.PowerIteration(wl["eps"], MAX_ITER, n, (n + 4095) // 4096)
     rank_t = torch.empty(n, dtype=torch.float32, device=device)

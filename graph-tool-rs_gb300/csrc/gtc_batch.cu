@@ -556,10 +556,10 @@ __global__ void k_gb_degree(uint32_t n, const uint32_t* __restrict__ push_off,
         const float oc = __shfl_xor_sync(0xffffffffu, k.c, o, 8);
         k.merge(os, oc);
     }
-    if (in && sub == 0) {
-        const double dg = wout ? (double)k.s + (double)k.c : (double)(push_off[v + 1] - push_off[v]);
-        invdeg[v] = dg != 0.0 ? (float)(1.0 / dg) : 0.f;
-        sink[v] = dg == 0.0 ? 1 : 0;
+    if (in && sub == 0) {  // FP32 only: a few FP64 operations per vertex cost more than its loads
+        const float dg = wout ? k.value() : (float)(push_off[v + 1] - push_off[v]);
+        invdeg[v] = dg != 0.f ? __frcp_rn(dg) : 0.f;
+        sink[v] = dg == 0.f ? 1 : 0;
     }
 }
 
