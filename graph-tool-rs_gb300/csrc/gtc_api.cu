@@ -28,6 +28,22 @@ static void require_device() {
     e = cudaFree(nullptr);  // the device's context exists before any handle is made
     if (e != cudaSuccess)
         throw Error{GTC_ERR_CUDA, std::string("context creation failed: ") + cudaGetErrorString(e)};
+    // Solves allocate their scratch from the device's default memory pool
+    // (cudaMallocAsync) and free it when they return.  With the pool's
+    // default release threshold (0) the freed memory goes back to the driver
+    // at the next synchronisation and the next solve maps it again; keeping
+    // it in this process's pool makes repeated solves reuse it.
+    static bool pool_kept[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && !pool_kept[dev]) {
+        cudaMemPool_t pool = nullptr;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) == cudaSuccess)
+                pool_kept[dev] = true;
+        }
+        (void)cudaGetLastError();
+    }
 }
 
 template <class F>
