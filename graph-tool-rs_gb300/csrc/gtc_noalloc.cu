@@ -2,9 +2,8 @@
 //
 // Who needs it: callers that cannot allocate device memory at the time they
 // run PageRank.  Examples are a host runtime that reserves all GPU memory up
-// front and forbids later allocations, and code that runs where an
-// allocation would stall or fail (a stream another framework is capturing, a
-// latency-critical path with no allocator calls allowed).  For them this
+// front and forbids later allocations, and a latency-critical path where no
+// allocator call is allowed because it could stall or fail.  For them this
 // entry point takes the graph (a CSC in device memory) and the output
 // buffer, and keeps every intermediate vector in one file-scope device
 // array compiled into the library.

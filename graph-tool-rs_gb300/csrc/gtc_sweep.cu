@@ -150,13 +150,30 @@ void build_units(const uint32_t* d_off, const uint32_t* d_other, const uint32_t*
     }
     u.n_slices = n_slices;
 
-    // ---- medium rows, in label order ----
+    // ---- medium rows, in label order, with their entry ranges ----
     scan_exclusive_u32(is_med.get(), pos.get(), n, s, &L);
     u.n_med = n ? fetch_u32(pos.get() + n, s) : 0;
     u.med.alloc(u.n_med, s);
+    std::vector<uint32_t> mrows(u.n_med), moff(2 * (size_t)u.n_med);
     if (u.n_med) {
         k_compact_u32<<<gn, TB, 0, s>>>(n, is_med.get(), pos.get(), nullptr, u.med.get());
         GTC_LAUNCHED();
+        DevBuf<uint32_t> dmo(2 * (size_t)u.n_med, s);
+        k_row_bounds<<<grid_for(u.n_med, TB, 1u << 30), TB, 0, s>>>(u.n_med, u.med.get(), d_off,
+                                                                     dmo.get());
+        GTC_LAUNCHED();
+        GTC_CUDA(cudaMemcpyAsync(mrows.data(), u.med.get(), (size_t)u.n_med * 4,
+                                 cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaMemcpyAsync(moff.data(), dmo.get(), (size_t)u.n_med * 8,
+                                 cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+    }
+    // the slices' first entries, for their work items
+    std::vector<uint32_t> soff((size_t)n_slices + 1, 0u);
+    if (n_slices) {
+        GTC_CUDA(cudaMemcpyAsync(soff.data(), u.slice_off.get(), ((size_t)n_slices + 1) * 4,
+                                 cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
     }
 
     // ---- long rows: chunk table on the host ----
@@ -186,8 +203,10 @@ void build_units(const uint32_t* d_off, const uint32_t* d_other, const uint32_t*
         for (uint32_t c = 0; c < chunks; ++c) units.push_back(make_uint4(UNIT_LONG, k, c, 0));
         slot += chunks;
     }
-    for (uint32_t q = 0; q < u.n_med; ++q) units.push_back(make_uint4(UNIT_MEDIUM, q, 0, 0));
-    for (uint32_t k = 0; k < n_slices; ++k) units.push_back(make_uint4(UNIT_SLICES, k, 0, 0));
+    for (uint32_t q = 0; q < u.n_med; ++q)
+        units.push_back(make_uint4(UNIT_MEDIUM, mrows[q], moff[2 * (size_t)q], moff[2 * (size_t)q + 1]));
+    for (uint32_t k = 0; k < n_slices; ++k)
+        units.push_back(make_uint4(UNIT_SLICES, k, soff[k], (soff[k + 1] - soff[k]) >> 5));
 
     u.n_units = (uint32_t)units.size();
     u.n_long = (uint32_t)longs.size();

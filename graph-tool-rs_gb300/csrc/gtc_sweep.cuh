@@ -39,10 +39,10 @@ constexpr int SP_SLICE_MAX = 128;   // longest row kept in a slice
 constexpr int SP_WINDOW = 2048;     // rows sorted by length inside windows of this many
 constexpr uint32_t NO_ROW = 0xFFFFFFFFu;
 
-// Work items, one warp each (uint4.x = kind; .y/.z as described).
+// Work items, one warp each (uint4.x = kind; .y/.z/.w as described).
 constexpr uint32_t UNIT_LONG = 1;    // long row index y, chunk z
-constexpr uint32_t UNIT_MEDIUM = 2;  // medium row med[y]
-constexpr uint32_t UNIT_SLICES = 3;  // slice y
+constexpr uint32_t UNIT_MEDIUM = 2;  // row y, its entries [z, w) of the pull half
+constexpr uint32_t UNIT_SLICES = 3;  // slice y, first sliced entry z, w steps of 32
 
 // Cut the rows of a pull half into the three tiers and the work list.
 void build_units(const uint32_t* d_off, const uint32_t* d_other, const uint32_t* d_eid,
@@ -113,43 +113,72 @@ struct KahanLite {
 // The per-row epilogue.  PageRank: (a, b) = (|nv - prev|, dangling mass of
 // next).  Eigenvector: a = s^2 (the squared norm), next = s unnormalised.
 // Streamed once per sweep: loaded and stored evict-first (.cs), so the
-// gathered vector is what stays in L2.
+// gathered vector is what stays in L2.  The row's own operands are loaded
+// by row_load as soon as the row is known -- before its gathers -- so their
+// latency overlaps the gathers instead of following them.
+struct RowIn {
+    float prev = 0.f, invdeg = 0.f, pers = 0.f, g = 0.f;
+    bool sink = false, active = true;
+};
+
 template <int MODE>
-__device__ __forceinline__ void sweep_row(const SweepArgs& A, uint32_t v, float sum, float psink,
-                                          float& ta, float& tb) {
-    if (A.active && !A.active[v]) {
-        A.next[v] = A.prev[v];
+__device__ __forceinline__ RowIn row_load(const SweepArgs& A, uint32_t v) {
+    RowIn r;
+    if (A.active) r.active = A.active[v] != 0;
+    if (MODE != MODE_EIGEN)
+        r.prev = __ldcs(A.prev + v);
+    else if (!r.active)  // eigenvector reads prev only to carry an inactive row
+        r.prev = A.prev[v];
+    if (MODE != MODE_EIGEN) {
+        r.invdeg = __ldcs(A.invdeg + v);
+        r.sink = __ldcs(A.sink + v) != 0;
+        r.pers = A.pers ? __ldcs(A.pers + v) : A.uniform;
+    }
+    if (MODE == MODE_ADJOINT) r.g = __ldcs(A.gvec + v);
+    return r;
+}
+
+template <int MODE>
+__device__ __forceinline__ void row_finish(const SweepArgs& A, uint32_t v, const RowIn& in,
+                                           float sum, float psink, float& ta, float& tb) {
+    if (!in.active) {
+        A.next[v] = in.prev;
         if (MODE == MODE_PAGERANK) A.ynext[v] = 0.f;
         ta = 0.f, tb = 0.f;
         return;
     }
     if (MODE == MODE_PAGERANK) {
-        const float pv = A.pers ? __ldcs(A.pers + v) : A.uniform;
+        const float pv = in.pers;
         const float r = __fadd_rn(__fmul_rn(psink, pv), sum);
         const float nv = __fadd_rn(__fmul_rn(A.one_minus_d, pv), __fmul_rn(A.d, r));
         __stcs(A.next + v, nv);
-        A.ynext[v] = __fmul_rn(nv, __ldcs(A.invdeg + v));
-        ta = fabsf(__fsub_rn(nv, __ldcs(A.prev + v)));
-        tb = __ldcs(A.sink + v) ? nv : 0.f;
+        A.ynext[v] = __fmul_rn(nv, in.invdeg);
+        ta = fabsf(__fsub_rn(nv, in.prev));
+        tb = in.sink ? nv : 0.f;
     } else if (MODE == MODE_ADJOINT) {
         // The iterate is mu + alpha (a shift along the all-ones vector, which
         // the transposed map keeps: A^T 1 = 1 off the sinks).  sum = sum over
         // v's out-edges of w * mu[t], so (A^T (mu + alpha))_v = at + alpha off
         // the sinks, and a sink takes p . (mu + alpha) = tau.
-        const float at = __fmul_rn(__ldcs(A.invdeg + v), sum);
-        const float dn = __fadd_rn(at, __ldcs(A.sink + v) ? A.tau : A.alpha);
-        const float nv = __fadd_rn(__ldcs(A.gvec + v), __fmul_rn(A.d, dn));
+        const float at = __fmul_rn(in.invdeg, sum);
+        const float dn = __fadd_rn(at, in.sink ? A.tau : A.alpha);
+        const float nv = __fadd_rn(in.g, __fmul_rn(A.d, dn));
         __stcs(A.next + v, nv);
         A.ynext[v] = at;  // kept for the weight gradient
         // the fixed-point residual of the shifted iterate
-        ta = fabsf(__fsub_rn(__fsub_rn(nv, __ldcs(A.prev + v)), A.alpha));
-        const float pv = A.pers ? __ldcs(A.pers + v) : A.uniform;
-        tb = __fmul_rn(pv, nv);  // p . (next iterate, before its shift)
+        ta = fabsf(__fsub_rn(__fsub_rn(nv, in.prev), A.alpha));
+        tb = __fmul_rn(in.pers, nv);  // p . (next iterate, before its shift)
     } else {
         A.next[v] = sum;
         ta = __fmul_rn(sum, sum);
         tb = 0.f;
     }
+}
+
+template <int MODE>
+__device__ __forceinline__ void sweep_row(const SweepArgs& A, uint32_t v, float sum, float psink,
+                                          float& ta, float& tb) {
+    row_finish<MODE>(A, v, row_load<MODE>(A, v), sum, psink, ta, tb);
 }
 
 template <bool HOT>
@@ -193,12 +222,15 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
     const uint32_t n_buckets = (A.n_units + SP_BUCKET - 1) / SP_BUCKET;
     for (uint32_t bk = gw; bk < n_buckets; bk += nw) {
     KahanLite bucket_a, bucket_b;
+    // the next item's descriptor is loaded while this item runs
+    uint4 Unext = __ldg(A.units + bk);
     for (uint32_t u = bk; u < A.n_units; u += n_buckets) {
-        const uint4 U = A.units[u];
+        const uint4 U = Unext;
+        if (u + n_buckets < A.n_units) Unext = __ldg(A.units + u + n_buckets);
         if (U.x == UNIT_SLICES) {
-            const uint32_t k = U.y;
-            const uint32_t b = __ldg(A.slice_off + k);
-            const uint32_t len = (__ldg(A.slice_off + k + 1) - b) >> 5;
+            // {kind, slice, first entry, steps}: no table lookup before the
+            // index stream starts
+            const uint32_t k = U.y, b = U.z, len = U.w;
             const uint32_t row = __ldg(A.slice_rows + 32 * k + lane);
             const uint32_t* ip = A.sidx + b + lane;
             const float* wp = WEIGHTED ? A.sw + b + lane : nullptr;
@@ -228,10 +260,12 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
                 acc.add(v2);
                 acc.add(v3);
             };
+            RowIn rin;
             if (len >= 4) {
                 uint32_t s0 = __ldcs(ip), s1 = __ldcs(ip + 32), s2 = __ldcs(ip + 64),
                          s3 = __ldcs(ip + 96);
                 ip += 128;
+                if (row != NO_ROW) rin = row_load<MODE>(A, row);
                 for (; j + 8 <= len; j += 4) {
                     const uint32_t n0 = __ldcs(ip), n1 = __ldcs(ip + 32), n2 = __ldcs(ip + 64),
                                    n3 = __ldcs(ip + 96);
@@ -241,6 +275,9 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
                 }
                 step(s0, s1, s2, s3);
                 j += 4;
+            }
+            else if (row != NO_ROW) {
+                rin = row_load<MODE>(A, row);
             }
             for (; j < len; ++j) {
                 float v = gather<HOT>(A, hot, __ldcs(ip));
@@ -253,7 +290,7 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
             }
             if (row != NO_ROW) {
                 float ta, tb;
-                sweep_row<MODE>(A, row, acc.value(), psink, ta, tb);
+                row_finish<MODE>(A, row, rin, acc.value(), psink, ta, tb);
                 bucket_a.add(ta);
                 bucket_b.add(tb);
             }
@@ -261,9 +298,11 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
             // a medium row, or one chunk of a long row: lanes stride entries
             uint32_t row, b, e;
             uint4 LR = make_uint4(0, 0, 0, 0);
+            RowIn rin;
             if (U.x == UNIT_MEDIUM) {
-                row = __ldg(A.med + U.y);
-                b = __ldg(A.off + row), e = __ldg(A.off + row + 1);
+                // {kind, row, first entry, end}
+                row = U.y, b = U.z, e = U.w;
+                rin = row_load<MODE>(A, row);
             } else {
                 LR = A.longs[U.y];
                 row = LR.x;
@@ -298,7 +337,7 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
             if (U.x == UNIT_MEDIUM) {
                 if (lane == 0) {
                     float ta, tb;
-                    sweep_row<MODE>(A, row, k.value(), psink, ta, tb);
+                    row_finish<MODE>(A, row, rin, k.value(), psink, ta, tb);
                     bucket_a.add(ta);
                     bucket_b.add(tb);
                 }
