@@ -16,7 +16,7 @@ static thread_local std::string t_err;
 
 void set_error(const std::string& msg) { t_err = msg; }
 
-static void require_device() {
+void require_device() {
     int count = 0;
     cudaError_t e = cudaGetDeviceCount(&count);
     if (e != cudaSuccess || count == 0) {

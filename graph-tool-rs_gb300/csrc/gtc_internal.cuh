@@ -21,6 +21,10 @@ namespace gtc {
 // Per-thread message of the last failing call (gtc_last_error()).
 void set_error(const std::string& msg);
 
+// Throws GTC_ERR_NO_DEVICE unless a CUDA device is usable (and makes its
+// context current).
+void require_device();
+
 struct Error {
     int status;
     std::string msg;

@@ -8,7 +8,10 @@ on one NVIDIA GB300, behind the reference's Python module surface.
 
     from graph_tool.centrality import pagerank
     rank = pagerank(g)                        # graph-tool's signature
+
+    g = load_graph("karate.gt")               # .gt reader, adjacency decoded on the GPU
 """
 from ._rust import Graph, GraphBatch, PropertyMap, value_types  # noqa: F401
+from .gt import GtFile, load_graph  # noqa: F401
 
-__all__ = ["Graph", "GraphBatch", "PropertyMap", "value_types"]
+__all__ = ["Graph", "GraphBatch", "PropertyMap", "value_types", "GtFile", "load_graph"]

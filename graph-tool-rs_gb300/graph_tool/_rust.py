@@ -109,6 +109,16 @@ class Graph:
         self._m = 0
         self._handle = None
         self._flat = None
+        self._lazy = False  # edges live only in the handle (a graph read by load_graph)
+        self.directed = True
+
+    @classmethod
+    def _from_handle(cls, handle, n: int, m: int) -> "Graph":
+        """Adopt a gtc_graph built elsewhere (the .gt reader); its edge list
+        is copied back from the device only when asked for."""
+        g = cls()
+        g._n, g._m, g._handle, g._lazy = int(n), int(m), handle, True
+        return g
 
     # ---- size ---------------------------------------------------------
     def num_vertices(self) -> int:
@@ -122,6 +132,8 @@ class Graph:
 
     # ---- mutation -----------------------------------------------------
     def _dirty(self):
+        if self._lazy:
+            self.edges()  # the handle is the only copy of the edges so far
         self._flat = None
         if self._handle is not None:
             _ffi.check(_ffi.lib().gtc_graph_destroy(self._handle))
@@ -171,6 +183,14 @@ class Graph:
 
     def edges(self):
         """(src, tgt) arrays indexed by edge index."""
+        if self._lazy:
+            # every out-half entry (other, idx) of vertex v is edge idx: v -> other
+            oo, ot, oi, _, _, _ = self.blocks()
+            src = np.empty(self._m, np.uint32)
+            tgt = np.empty(self._m, np.uint32)
+            src[oi] = np.repeat(np.arange(self._n, dtype=np.uint32), np.diff(oo).astype(np.int64))
+            tgt[oi] = ot
+            self._src, self._tgt, self._lazy = [src], [tgt], False
         if self._flat is None:
             if self._src:
                 self._flat = (np.concatenate(self._src), np.concatenate(self._tgt))

@@ -162,6 +162,58 @@ int gtc_graph_export(const gtc_graph* g, uint64_t* out_off, uint32_t* out_other,
  * handle's own stream). */
 int gtc_graph_set_stream(gtc_graph* g, void* stream);
 
+/* ---- the .gt file format -----------------------------------------------
+ *
+ * Replaces gt_io::gt::read (crates/gt-io/src/gt.rs:555-626, read_adjacency
+ * :628-678, read_column :724-820) for graphs headed for the solvers.
+ *
+ * gtc_gt_open parses the framing of a .gt document held in host memory
+ * (bytes[0 .. len), copied into the handle): header, one record per vertex,
+ * property table.  Everything a field declares must lie inside the
+ * document.  Errors (all GTC_ERR_ARG, the message names the byte offset
+ * where one applies): a bad magic or a short head, a version other than 1,
+ * truncation anywhere, a vertex or edge count beyond the index space, a
+ * property domain above 2, a value-type index above 14, a name or a string
+ * value that is not UTF-8.  Vertex indices inside the lists are checked by
+ * gtc_gt_graph, on the device.
+ *
+ * Property kinds are the indices of ValueKind::ALL
+ * (crates/gt-core/src/prop/value.rs:79-95): 0 bool, 1 int16, 2 int32,
+ * 3 int64, 4 double, 5 long double, 6 string, 7-13 the vector kinds,
+ * 14 python object.  Domains: 0 graph (1 value), 1 vertex (n), 2 edge (m);
+ * an edge column's i-th value belongs to edge i (gt.rs:44-58). */
+typedef struct gtc_gt_file gtc_gt_file;
+
+int gtc_gt_open(const uint8_t* bytes, uint64_t len, gtc_gt_file** out);
+int gtc_gt_close(gtc_gt_file* f);
+
+/* Vertices, edges, the directed flag, the byte-order flag of the document,
+ * and the number of properties. */
+int gtc_gt_info(const gtc_gt_file* f, uint64_t* n, uint64_t* m, int32_t* directed,
+                int32_t* big_endian, uint64_t* nprops);
+
+/* The header comment (valid while the handle lives). */
+int gtc_gt_comment(const gtc_gt_file* f, const char** text, uint64_t* len);
+
+/* Property i: name (valid while the handle lives), domain, kind and number
+ * of values. */
+int gtc_gt_property(const gtc_gt_file* f, uint64_t i, const char** name, uint64_t* name_len,
+                    int32_t* domain, int32_t* kind, uint64_t* count);
+
+/* The values of a numeric scalar column (kinds 0-4) as doubles; out_len >=
+ * the column's count.  Other kinds are GTC_ERR_ARG. */
+int gtc_gt_property_f64(const gtc_gt_file* f, uint64_t i, double* out, uint64_t out_len);
+
+/* The column's bytes exactly as stored (in the document's byte order). */
+int gtc_gt_property_bytes(const gtc_gt_file* f, uint64_t i, const uint8_t** data, uint64_t* len);
+
+/* The graph of the document: its lists are decoded on the device and
+ * replayed as add_edge(v, u) for every vertex v in order and every entry u of
+ * v's list in file order (gt.rs:648-674), so edge k is the document's k-th
+ * list entry and every block matches the reference reader's.  An index not
+ * below n is GTC_ERR_INDEX, naming the first such index in file order. */
+int gtc_gt_graph(const gtc_gt_file* f, gtc_graph** out);
+
 /* ---- centrality ------------------------------------------------------- */
 
 /* PageRank: pagerank (pers == NULL) and pagerank_with (pers != NULL),
@@ -327,9 +379,10 @@ int gtc_pagerank_adjoint_device(gtc_graph* g, const gtc_view* view, const gtc_dv
  * FP32 vectors, compensated row sums, FP64 delta and dangling mass.  All
  * calls share the static array and it keeps the last call's contents (each
  * call clears what must start at zero); calls that overlap on the GPU race.
- * The first call on a device looks the array's device address up, so make it
- * before anything that must not see that call's synchronisation.  Returns
- * when the result is in d_rank. */
+ * The first call on a device does a one-time set-up: it looks the array's
+ * device address up (cudaGetSymbolAddress with that device current).  Make
+ * that first call before any stream capture.  Returns when the result is in
+ * d_rank. */
 int gtc_pagerank_noalloc(uint64_t n, const uint32_t* d_off, const uint32_t* d_src,
                          const uint32_t* d_out_degree, double damping, double epsilon,
                          uint64_t max_iter, float* d_rank, uint64_t* iters_out, void* stream);
