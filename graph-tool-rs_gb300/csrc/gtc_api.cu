@@ -317,6 +317,21 @@ int gtc_pagerank(gtc_graph* g, const gtc_view* view, const double* weight, uint6
     });
 }
 
+int gtc_betweenness(gtc_graph* g, const gtc_view* view, int32_t undirected, double* vertex_bc,
+                    uint64_t vertex_len, double* edge_bc, uint64_t edge_len,
+                    const gtc_options* opt, gtc_result* result) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        GTC_REQUIRE(!vertex_bc || vertex_len >= g->n, GTC_ERR_ARG,
+                    "vertex map is shorter than the vertex bound");
+        GTC_REQUIRE(!edge_bc || edge_len >= g->m, GTC_ERR_ARG,
+                    "edge map is shorter than the edge bound");
+        gtc_result r{};
+        gtc::betweenness(g, view, undirected != 0, vertex_bc, edge_bc, &r, stream_of(g, opt));
+        if (result) *result = r;
+    });
+}
+
 int gtc_eigenvector(gtc_graph* g, const gtc_view* view, const double* weight, uint64_t weight_len,
                     const gtc_power_iteration* params, double* x, uint64_t x_len, uint64_t x_had,
                     const gtc_options* opt, gtc_result* result) {

@@ -83,6 +83,32 @@ struct PprArgs {
     int* err;          // set when a bounded wait gave up
 };
 
+// Two FP32 lanes per instruction (add/sub/mul.rn.f32x2, sm_100 and later):
+// each half is the IEEE round-to-nearest operation of its own operands, so a
+// pair operation gives bit for bit the two scalar results, in half the
+// instructions.  The per-slot sums below are issue-bound, so they use pairs.
+__device__ __forceinline__ void f2_add(float& dx, float& dy, float ax, float ay, float bx,
+                                       float by) {
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "add.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(dx), "=f"(dy)
+        : "f"(ax), "f"(ay), "f"(bx), "f"(by));
+}
+__device__ __forceinline__ void f2_sub(float& dx, float& dy, float ax, float ay, float bx,
+                                       float by) {
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "sub.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(dx), "=f"(dy)
+        : "f"(ax), "f"(ay), "f"(bx), "f"(by));
+}
+__device__ __forceinline__ void f2_mul(float& dx, float& dy, float ax, float ay, float bx,
+                                       float by) {
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "mul.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(dx), "=f"(dy)
+        : "f"(ax), "f"(ay), "f"(bx), "f"(by));
+}
+
 // Classic Kahan accumulation of C slots (value s - c).
 template <int C>
 struct Acc {
@@ -97,7 +123,34 @@ struct Acc {
         c[k] = __fsub_rn(__fsub_rn(t, s[k]), y);
         s[k] = t;
     }
+    // slots k and k + 1 at once, the same operations as two add() calls
+    __device__ __forceinline__ void add2(int k, float x0, float x1) {
+        float y0, y1, t0, t1, u0, u1;
+        f2_sub(y0, y1, x0, x1, c[k], c[k + 1]);
+        f2_add(t0, t1, s[k], s[k + 1], y0, y1);
+        f2_sub(u0, u1, t0, t1, s[k], s[k + 1]);
+        f2_sub(c[k], c[k + 1], u0, u1, y0, y1);
+        s[k] = t0, s[k + 1] = t1;
+    }
+    // every slot: pairs, and the last one alone when C is odd
+    __device__ __forceinline__ void add_all(const float (&x)[C]) {
+#pragma unroll
+        for (int q = 0; q + 1 < C; q += 2) add2(q, x[q], x[q + 1]);
+        if (C % 2) add(C - 1, x[C - 1]);
+    }
 };
+
+// t[q] += x[q] (W: x[q] * w) for every slot, in pairs.
+template <int C, bool W>
+__device__ __forceinline__ void slots_accumulate(float (&t)[C], const float (&x)[C], float w) {
+#pragma unroll
+    for (int q = 0; q + 1 < C; q += 2) {
+        float a = x[q], b = x[q + 1];
+        if (W) f2_mul(a, b, a, b, w, w);
+        f2_add(t[q], t[q + 1], t[q], t[q + 1], a, b);
+    }
+    if (C % 2) t[C - 1] = __fadd_rn(t[C - 1], W ? __fmul_rn(x[C - 1], w) : x[C - 1]);
+}
 
 // The slots of a lane.  A row of S = 32 * C slots is read by the warp as C
 // / V vector loads of V floats per lane (V = 4 when C is a multiple of 4, 2
@@ -480,11 +533,9 @@ __global__ void __launch_bounds__(PB_NT) k_ppr_bulk(PprArgs A) {
                     const float ww = W ? __shfl_sync(0xffffffffu, wC, i) : 1.f;
                     float x[C];
                     Lanes<C>::template load<false>(rb + (size_t)i * S, lane, x);
-#pragma unroll
-                    for (int q = 0; q < C; ++q) t[q] = __fadd_rn(t[q], W ? __fmul_rn(x[q], ww) : x[q]);
+                    slots_accumulate<C, W>(t, x, ww);
                 }
-#pragma unroll
-                for (int q = 0; q < C; ++q) acc.add(q, t[q]);
+                acc.add_all(t);
             }
             if (bC.last) {
                 if (bC.it < A.n_chunks) {

@@ -266,6 +266,30 @@ class Graph:
                    vfilt, efilt, precision, stream, True, plan_len)
         return r if result else (r.eigenvalue, r.iterations)
 
+    def betweenness(self, vertex_bc: PropertyMap | None = None,
+                    edge_bc: PropertyMap | None = None, undirected: bool = False,
+                    reversed: bool = False, vfilt=None, efilt=None, result: bool = False):
+        """betweenness (crates/gt-algo/src/centrality.rs:633-689): Brandes
+        from every vertex of the view, unnormalised; both maps are
+        overwritten.  ``undirected`` runs on the undirected view (halved).
+        Returns (vertex map, edge map)."""
+        vb = vertex_bc if vertex_bc is not None else self.new_vertex_property("double")
+        eb = edge_bc if edge_bc is not None else self.new_edge_property("double")
+        for m_, key in ((vb, "v"), (eb, "e")):
+            if not isinstance(m_, PropertyMap) or m_._g is not self or m_.key_type() != key \
+                    or m_.value_type() != "double":
+                raise ValueError("betweenness maps must be 'double' maps of this graph")
+        va, ea = vb.sized_for(), eb.sized_for()
+        vm = _mask(self, vfilt, self.num_vertices())
+        em = _mask(self, efilt, self.edge_index_range())
+        view = _ffi.View(int(bool(reversed)), 0, _ffi.ptr(vm, _ffi.u8p),
+                         0 if vm is None else vm.size, _ffi.ptr(em, _ffi.u8p),
+                         0 if em is None else em.size)
+        res = _ffi.Result()
+        _ffi.check(_ffi.lib().gtc_betweenness(
+            self.handle(), C.byref(view), int(bool(undirected)), _ffi.ptr(va, _ffi.f64p), va.size,
+            _ffi.ptr(ea, _ffi.f64p), ea.size, None, C.byref(res)))
+        return (vb, eb, res) if result else (vb, eb)
 
     def ppr_batch(self, seeds, values=None, weight: PropertyMap | None = None,
                   damping: float = 0.85, epsilon: float = 1e-6, max_iter: int = 0,

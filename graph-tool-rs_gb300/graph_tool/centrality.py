@@ -1,6 +1,6 @@
 """graph-tool's functional centrality interface over the GPU solves.
 
-``pagerank`` and ``eigenvector`` take graph-tool's keyword arguments
+``pagerank``, ``eigenvector`` and ``betweenness`` take graph-tool's keyword arguments
 (``graph_tool.centrality.pagerank(g, damping, pers, weight, prop, epsilon,
 max_iter, ret_iter)``) and call the same kernels as ``Graph.pagerank`` /
 ``Graph.eigenvector``: crates/gt-algo/src/centrality.rs:234-384 and :405-497
@@ -31,3 +31,10 @@ def eigenvector(g: Graph, weight: PropertyMap | None = None, vprop: PropertyMap 
     eig, _ = g.eigenvector(x, weight=weight, epsilon=epsilon, max_iter=max_iter or 0,
                            grain=grain, precision=precision)
     return eig, x
+
+
+def betweenness(g: Graph, vprop: PropertyMap | None = None, eprop: PropertyMap | None = None,
+                undirected: bool = False):
+    """(vertex betweenness, edge betweenness), unnormalised, every vertex a
+    pivot (crates/gt-algo/src/centrality.rs:633-689)."""
+    return g.betweenness(vprop, eprop, undirected=undirected)

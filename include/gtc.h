@@ -244,6 +244,21 @@ int gtc_eigenvector(gtc_graph* g, const gtc_view* view, const double* weight,
                     uint64_t weight_len, const gtc_power_iteration* params, double* x,
                     uint64_t x_len, uint64_t x_had, const gtc_options* opt, gtc_result* result);
 
+/* Betweenness centrality (Brandes), crates/gt-algo/src/centrality.rs:633-689:
+ * unweighted, every vertex of the view a source, unnormalised.  Both maps are
+ * overwritten (init_centrality_map): vertex_bc by vertex index (vertex_len >=
+ * vertex bound), edge_bc by EdgeId (edge_len >= edge bound); a vertex or edge
+ * outside the view gets 0; either pointer may be NULL to skip that map.
+ * undirected != 0 runs on the undirected view (Und,
+ * crates/gt-core/src/view/undirected.rs:106-125: every incident edge is an
+ * out-edge), whose maps are halved (centrality.rs:680-688).  FP64; path counts
+ * are exact below 2^53; sums are associated differently from the reference's
+ * (deterministic, within the reference tests' 1e-9 of it).
+ * result->iterations = sources run.  Host arrays. */
+int gtc_betweenness(gtc_graph* g, const gtc_view* view, int32_t undirected, double* vertex_bc,
+                    uint64_t vertex_len, double* edge_bc, uint64_t edge_len,
+                    const gtc_options* opt, gtc_result* result);
+
 /* Device variants: the same solves with every vector in device memory of
  * the handle's device (e.g. torch tensors), FP32 or FP64.  NULL or ptr ==
  * NULL means absent (Unity weights / uniform pers).  rank / x must be

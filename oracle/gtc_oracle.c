@@ -30,6 +30,9 @@
  *   - eigenvector                      crates/gt-algo/src/centrality.rs:405-497
  *   - Rev view (in <-> out)            crates/gt-core/src/view/reversed.rs:109-138
  *   - Filtered view (masks)            crates/gt-core/src/view/filtered.rs:299-319
+ *   - betweenness (Brandes)            crates/gt-algo/src/centrality.rs:499-689
+ *   - Und view (out_edges = all_edges)  crates/gt-core/src/view/undirected.rs:106-125,
+ *                                      crates/gt-core/src/adj/list.rs:170-175
  */
 #include <math.h>
 #include <stdint.h>
@@ -589,6 +592,148 @@ int64_t ora_eigenvector(const ora_graph *g, int reversed, const uint8_t *vmask,
     *eig = norm;
     free(active), free(scratch), free(partials);
     return (int64_t)iter;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Betweenness (Brandes), centrality.rs:499-689                              */
+/* ------------------------------------------------------------------------ */
+
+/* The edges a source's BFS walks from u: out_edges of the directed view, or
+ * the whole block (out-half then in-half) for the undirected view. */
+static inline void bc_edges(const ora_view *w, int undirected, uint64_t u, const ora_entry **b,
+                            const ora_entry **e) {
+    if (undirected) {
+        const ora_block *bl = &w->g->blocks[u];
+        *b = bl->e;
+        *e = bl->e + bl->len;
+    } else {
+        half(w, u, 0, b, e);
+    }
+}
+
+typedef struct {
+    uint64_t v;  /* predecessor */
+    uint32_t e;  /* edge */
+} bc_pred;
+
+/* Brandes::run for one source (centrality.rs:544-610): BFS in dequeue order,
+ * predecessors pushed in discovery order, then the dependency accumulation
+ * over the dequeue order reversed. */
+static void bc_run(const ora_view *w, int undirected, const uint64_t *verts, uint64_t nverts,
+                   uint64_t s, int64_t *dist, double *sigma, double *dep, bc_pred **inc,
+                   uint64_t *inc_len, uint64_t *inc_cap, uint64_t *order, double *vb,
+                   double *eb) {
+    for (uint64_t k = 0; k < nverts; ++k) {
+        uint64_t i = verts[k];
+        inc_len[i] = 0;
+        sigma[i] = 0.0;
+        dep[i] = 0.0;
+        dist[i] = -1;
+    }
+    uint64_t head = 0, tail = 0;
+    sigma[s] = 1.0;
+    dist[s] = 0;
+    order[tail++] = s;  /* the order array doubles as the FIFO queue */
+    while (head < tail) {
+        uint64_t u = order[head++];
+        int64_t du = dist[u];
+        double su = sigma[u];
+        const ora_entry *b, *e;
+        bc_edges(w, undirected, u, &b, &e);
+        for (const ora_entry *x = b; x < e; ++x) {
+            if (!keep_inc(w, *x)) continue;
+            uint64_t t = x->other;
+            if (t == u) continue; /* a self-loop never shortens a path */
+            int tree = 0;
+            if (dist[t] < 0) { /* tree_edge: first discovery */
+                dist[t] = du + 1;
+                sigma[t] = su;
+                tree = 1;
+            } else if (dist[t] == du + 1) { /* non_tree_edge on a shortest path */
+                sigma[t] += su;
+            } else {
+                continue;
+            }
+            if (inc_len[t] == inc_cap[t]) {
+                uint64_t nc = inc_cap[t] ? 2 * inc_cap[t] : 4;
+                inc[t] = (bc_pred *)realloc(inc[t], nc * sizeof(bc_pred));
+                inc_cap[t] = nc;
+            }
+            inc[t][inc_len[t]].v = u;
+            inc[t][inc_len[t]].e = x->idx;
+            inc_len[t]++;
+            if (tree) order[tail++] = t;
+        }
+    }
+    for (uint64_t k = tail; k-- > 0;) {
+        uint64_t u = order[k];
+        double su = sigma[u];
+        for (uint64_t j = 0; j < inc_len[u]; ++j) {
+            uint64_t v = inc[u][j].v;
+            double factor = (sigma[v] / su) * (1.0 + dep[u]);
+            dep[v] += factor;
+            eb[inc[u][j].e] += factor;
+        }
+        if (u != s) vb[u] += dep[u];
+    }
+}
+
+/* betweenness(g, vertex_bc, edge_bc), centrality.rs:633-689: every vertex of
+ * the view is a source; sources are cut by Plan::new(|V|, ceil(|V|/16)) and
+ * each chunk's partial maps are folded in chunk order; an undirected run is
+ * halved.  vb has n entries, eb edge_bound entries; both are overwritten. */
+int ora_betweenness(const ora_graph *g, int reversed, int undirected, const uint8_t *vmask,
+                    const uint8_t *emask, double *vb, double *eb, int threads) {
+    ora_view w = {g, reversed, vmask, emask};
+    const uint64_t n = g->n, ne = g->next_id;
+    uint64_t nverts = 0;
+    uint64_t *verts = (uint64_t *)malloc((n ? n : 1) * sizeof(uint64_t));
+    if (!verts) return ORA_ERR_OOM;
+    for (uint64_t v = 0; v < n; ++v)
+        if (keep_v(&w, v)) verts[nverts++] = v;
+    /* Plan::new(|V|, max(ceil(|V| / BETWEENNESS_CHUNKS), 1)), centrality.rs:115, 654 */
+    uint64_t grain = (nverts + 15) / 16;
+    ora_plan plan = plan_new(nverts, grain ? grain : 1);
+    double *pv = (double *)calloc(plan.chunks * (n ? n : 1), sizeof(double));
+    double *pe = (double *)calloc(plan.chunks * (ne ? ne : 1), sizeof(double));
+    if (!pv || !pe) {
+        free(verts), free(pv), free(pe);
+        return ORA_ERR_OOM;
+    }
+#ifdef _OPENMP
+    if (threads < 1) threads = 1;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
+#endif
+    for (int64_t k = 0; k < (int64_t)plan.chunks; ++k) {
+        uint64_t lo, hi;
+        plan_range(plan, (uint64_t)k, &lo, &hi);
+        uint64_t nn = n ? n : 1;
+        int64_t *dist = (int64_t *)malloc(nn * sizeof(int64_t));
+        double *sigma = (double *)malloc(nn * sizeof(double));
+        double *dep = (double *)malloc(nn * sizeof(double));
+        bc_pred **inc = (bc_pred **)calloc(nn, sizeof(bc_pred *));
+        uint64_t *inc_len = (uint64_t *)calloc(nn, sizeof(uint64_t));
+        uint64_t *inc_cap = (uint64_t *)calloc(nn, sizeof(uint64_t));
+        uint64_t *order = (uint64_t *)malloc(nn * sizeof(uint64_t));
+        for (uint64_t q = lo; q < hi; ++q)
+            bc_run(&w, undirected, verts, nverts, verts[q], dist, sigma, dep, inc, inc_len,
+                   inc_cap, order, pv + (uint64_t)k * n, pe + (uint64_t)k * ne);
+        for (uint64_t i = 0; i < nn; ++i) free(inc[i]);
+        free(dist), free(sigma), free(dep), free(inc), free(inc_len), free(inc_cap), free(order);
+    }
+    (void)threads; /* used by the OpenMP pragma only */
+    for (uint64_t i = 0; i < n; ++i) vb[i] = 0.0;
+    for (uint64_t i = 0; i < ne; ++i) eb[i] = 0.0;
+    for (uint64_t k = 0; k < plan.chunks; ++k) {
+        for (uint64_t i = 0; i < n; ++i) vb[i] += pv[k * n + i];
+        for (uint64_t i = 0; i < ne; ++i) eb[i] += pe[k * ne + i];
+    }
+    if (undirected) {
+        for (uint64_t i = 0; i < n; ++i) vb[i] /= 2.0;
+        for (uint64_t i = 0; i < ne; ++i) eb[i] /= 2.0;
+    }
+    free(verts), free(pv), free(pe);
+    return ORA_OK;
 }
 
 /* Number of OpenMP threads the library was built to use (1 without OpenMP). */

@@ -59,6 +59,9 @@ def lib():
         L.ora_eigenvector.argtypes = [C.c_void_p, C.c_int, _u8p, _u8p, _f64p, C.c_double,
                                       C.c_uint64, C.c_uint64, C.c_uint64, _f64p, C.c_uint64,
                                       C.c_int, _f64p]
+        L.ora_betweenness.restype = C.c_int
+        L.ora_betweenness.argtypes = [C.c_void_p, C.c_int, C.c_int, _u8p, _u8p, _f64p, _f64p,
+                                      C.c_int]
         L.ora_last_error.restype = C.c_char_p
         L.ora_max_threads.restype = C.c_int
         L.ora_plan_range.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, _u64p, _u64p]
@@ -192,6 +195,19 @@ class Graph:
         if it < 0:
             raise OracleError(lib().ora_last_error().decode())
         return out, eig.value, it
+
+    def betweenness(self, undirected=False, reversed=False, vmask=None, emask=None, threads=1):
+        """betweenness (centrality.rs:633-689) of the view (Und when
+        ``undirected``).  Returns (vertex f64[n], edge f64[edge bound])."""
+        vb = np.zeros(max(self.n, 1), np.float64)
+        eb = np.zeros(max(self.edge_bound(), 1), np.float64)
+        vm = None if vmask is None else np.ascontiguousarray(vmask, np.uint8)
+        em = None if emask is None else np.ascontiguousarray(emask, np.uint8)
+        st = lib().ora_betweenness(self._h, int(reversed), int(undirected), _ptr(vm, _u8p),
+                                   _ptr(em, _u8p), _ptr(vb, _f64p), _ptr(eb, _f64p), threads)
+        if st != 0:
+            raise OracleError("betweenness: out of memory")
+        return vb[:self.n], eb[:self.edge_bound()]
 
 
 def max_threads() -> int:

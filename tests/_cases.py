@@ -54,6 +54,12 @@ class OracleSolver:
     def blocks(self, n, src, tgt):
         return self.graph(n, src, tgt).export()
 
+    def betweenness(self, n, src, tgt, undirected=False, reversed=False, vmask=None,
+                    emask=None):
+        return self.graph(n, src, tgt).betweenness(undirected=undirected, reversed=reversed,
+                                                   vmask=vmask, emask=emask,
+                                                   threads=self.threads)
+
 
 class GpuSolver:
     """The GPU library through its C ABI (graph_tool._rust over ctypes)."""
@@ -102,6 +108,14 @@ class GpuSolver:
 
     def blocks(self, n, src, tgt):
         return self.graph(n, src, tgt).blocks()
+
+    def betweenness(self, n, src, tgt, undirected=False, reversed=False, vmask=None,
+                    emask=None):
+        g = self.graph(n, src, tgt)
+        vb, eb = g.new_vertex_property("double"), g.new_edge_property("double")
+        g.betweenness(vb, eb, undirected=undirected, reversed=reversed, vfilt=vmask,
+                      efilt=emask)
+        return vb.a.copy(), eb.a.copy()
 
 
 # --------------------------------------------------------------------------
@@ -275,3 +289,109 @@ def case_unity_is_general(S, thousand):
         assert ia == ib and a.tobytes() == b.tobytes()
     else:
         assert np.max(np.abs(a - b)) < 1e-7
+
+
+# --------------------------------------------------------------------------
+# betweenness (u16_centrality.rs:620-883)
+# --------------------------------------------------------------------------
+
+def brandes_flat(n, edges, directed):
+    """u16_centrality.rs:628-691: an independent Brandes over a flat edge list
+    (adjacency in edge order; an undirected edge listed at both endpoints),
+    unnormalised, halved when undirected."""
+    adj = [[] for _ in range(n)]
+    for ei, (s_, t_) in enumerate(edges):
+        adj[s_].append((t_, ei))
+        if not directed and s_ != t_:
+            adj[t_].append((s_, ei))
+    vb = [0.0] * n
+    eb = [0.0] * len(edges)
+    for s_ in range(n):
+        dist = [-1] * n
+        sigma = [0.0] * n
+        dep = [0.0] * n
+        pred = [[] for _ in range(n)]
+        order = [s_]
+        dist[s_], sigma[s_] = 0, 1.0
+        head = 0
+        while head < len(order):
+            u = order[head]
+            head += 1
+            for w, ei in adj[u]:
+                if w == u:
+                    continue
+                if dist[w] < 0:
+                    dist[w] = dist[u] + 1
+                    sigma[w] = sigma[u]
+                    pred[w].append((u, ei))
+                    order.append(w)
+                elif dist[w] == dist[u] + 1:
+                    sigma[w] += sigma[u]
+                    pred[w].append((u, ei))
+        for u in reversed(order):
+            for p, ei in pred[u]:
+                f = (sigma[p] / sigma[u]) * (1.0 + dep[u])
+                dep[p] += f
+                eb[ei] += f
+            if u != s_:
+                vb[u] += dep[u]
+    if not directed:
+        vb = [x / 2.0 for x in vb]
+        eb = [x / 2.0 for x in eb]
+    return np.array(vb), np.array(eb)
+
+
+def case_betweenness_random(S, cases=100):
+    """u16_centrality.rs:707-760: 100 small multigraphs with self-loops,
+    directed and undirected, within 1e-9 of the independent Brandes."""
+    from graph_tool.synth import SplitMix64
+    r = SplitMix64(0x0123_4567_89AB_CDEF)
+    for case in range(cases):
+        n = 3 + r.below(10)
+        m = r.below(3 * n + 1)
+        edges = [(r.below(n), r.below(n)) for _ in range(m)]
+        src, tgt = edges_of(edges) if m else (np.zeros(0, np.uint32), np.zeros(0, np.uint32))
+        for directed in (True, False):
+            gv, ge = S.betweenness(n, src, tgt, undirected=not directed)
+            wv, we = brandes_flat(n, edges, directed)
+            assert np.all(np.abs(gv - wv) < 1e-9), (case, directed, gv, wv)
+            assert np.all(np.abs(ge - we) < 1e-9), (case, directed, ge, we)
+
+
+def case_betweenness_path(S):
+    """u16_centrality.rs:767-792: on a 9-vertex path, vertex i has
+    i (n-1-i) and edge (i, i+1) has (i+1)(n-1-i), exactly."""
+    N = 9
+    src, tgt = edges_of([(i, i + 1) for i in range(N - 1)])
+    for undirected in (False, True):
+        gv, ge = S.betweenness(N, src, tgt, undirected=undirected)
+        assert gv.tolist() == [float(i * (N - 1 - i)) for i in range(N)]
+        assert ge.tolist() == [float((i + 1) * (N - 1 - i)) for i in range(N - 1)]
+
+
+def case_betweenness_back_edge(S):
+    """u16_centrality.rs:794-831: a 4-cycle with a chord, and its relabelling."""
+    edges = [(0, 1), (1, 2), (2, 3), (3, 0), (0, 2)]
+    gv, ge = S.betweenness(4, *edges_of(edges))
+    wv, we = brandes_flat(4, edges, True)
+    assert np.all(np.abs(gv - wv) < 1e-12) and np.all(np.abs(ge - we) < 1e-12)
+    hv, _ = S.betweenness(4, *edges_of([(3 - s_, 3 - t_) for s_, t_ in edges]))
+    assert np.all(np.abs(hv[::-1] - gv) < 1e-12)
+
+
+def case_betweenness_unreachable(S):
+    """u16_centrality.rs:870-883: no NaN from the unreachable half; the cut
+    vertex and the lone edge of the second component are exact."""
+    gv, ge = S.betweenness(6, *edges_of([(0, 1), (1, 2), (3, 4)]), undirected=True)
+    assert np.all(np.isfinite(gv))
+    assert gv[1] == 1.0 and gv[0] == 0.0 and gv[5] == 0.0
+    assert ge[2] == 1.0
+
+
+def ring_plus_chords(n=220, chords=600, seed=0xDEAD_BEEF_1234_5678):
+    """u16_centrality.rs:846-853: a ring plus random chords."""
+    from graph_tool.synth import SplitMix64
+    r = SplitMix64(seed)
+    edges = [(i, (i + 1) % n) for i in range(n)]
+    edges += [(r.below(n), r.below(n)) for _ in range(chords)]
+    return n, edges

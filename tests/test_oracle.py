@@ -161,3 +161,31 @@ def test_bad_vertex_is_an_error(oracle):
     g = oracle.Graph(2)
     with pytest.raises(oracle.OracleError, match="no such vertex"):
         g.add_edge(0, 5)
+
+
+# ---- betweenness (u16_centrality.rs:620-883) ------------------------------
+
+def test_betweenness_matches_an_independent_brandes(S):
+    K.case_betweenness_random(S)
+
+
+def test_betweenness_on_a_path_is_the_closed_form(S):
+    K.case_betweenness_path(S)
+
+
+def test_betweenness_back_edge_into_an_earlier_source(S):
+    K.case_betweenness_back_edge(S)
+
+
+def test_betweenness_unreachable_vertices_contribute_nothing(S):
+    K.case_betweenness_unreachable(S)
+
+
+def test_betweenness_bit_identical_across_thread_counts(oracle):
+    n, edges = K.ring_plus_chords()
+    g = oracle.Graph(n)
+    g.add_edge_arrays(*K.edges_of(edges))
+    base = g.betweenness(threads=1)
+    for t in (2, 4, 16):
+        got = g.betweenness(threads=t)
+        assert got[0].tobytes() == base[0].tobytes() and got[1].tobytes() == base[1].tobytes()
