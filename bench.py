@@ -25,7 +25,7 @@ edges x sweeps / seconds / 1e9.
   cpu_baseline  the CPU oracle (a C restatement of the reference's f64
             path, all host threads) on the same graph, bounded to a few sweeps.
 
-Two more measurements ride on the same line (skipped with --no-secondary):
+More measurements ride on the same line (skipped with --no-secondary):
 
   adjoint   gradient of L = c . pi (c ~ N(0,1)) with respect to FP32 edge
             weights U(0.1, 1) and a Dirichlet(1) personalisation on the same
@@ -39,8 +39,11 @@ Two more measurements ride on the same line (skipped with --no-secondary):
             blocks, p_in 16/n, p_out 2/n, FP32 weights U(0.1,1), epsilon 1e-6:
             one call solves every graph (a persistent kernel, replayed as a
             CUDA graph); graphs per second and edge-sweeps per second.
+  betweenness  Brandes from every vertex of an R-MAT scale-14 graph (edge
+            factor 16, deduplicated): GPU time against the CPU oracle on all
+            host threads, edges x sources per second, and their difference.
 
-``--section adjoint|ppr_batch|graph_batch`` runs one of them alone and prints
+``--section adjoint|ppr_batch|graph_batch|betweenness`` runs one of them alone and prints
 its JSON (``--ppr-scale``, ``--ppr-b``, ``--graphs`` shrink the last two for
 profiling; ``--workload`` picks the adjoint's graph).
 
@@ -421,6 +424,49 @@ def graph_batch_section(L, device, stream, G=4096):
             "cuda_graph_launches_per_solve": 1}
 
 
+def betweenness_section(L, device, stream, scale=14):
+    """Betweenness (Brandes, every vertex a source) of an R-MAT graph
+    (edge factor 16, deduplicated): the GPU (gtc_betweenness, host maps) and
+    the CPU oracle on all host threads, on the same graph.  Throughput is
+    edges x sources per second (the usual TEPS of all-sources betweenness)."""
+    import numpy as np
+    import oracle as O
+    from graph_tool import _ffi, synth
+    n, src, tgt = synth.rmat_cpu(scale, edge_factor=16, seed=7)
+    m = int(src.size)
+    h = C.c_void_p()
+    _ffi.check(L.gtc_graph_create(n, m, _ffi.ptr(src, _ffi.u32p), _ffi.ptr(tgt, _ffi.u32p),
+                                  C.byref(h)))
+    vb = np.zeros(n)
+    eb = np.zeros(m)
+    res = _ffi.Result()
+
+    def run():
+        _ffi.check(L.gtc_betweenness(h, None, 0, _ffi.ptr(vb, _ffi.f64p), n,
+                                     _ffi.ptr(eb, _ffi.f64p), m, None, C.byref(res)))
+
+    run()  # warm-up
+    t0 = time.perf_counter()
+    run()
+    wall = time.perf_counter() - t0
+    gpu_ms = float(res.device_ms)
+    _ffi.check(L.gtc_graph_destroy(h))
+    threads = os.cpu_count() or 1
+    og = O.Graph(n)
+    og.add_edge_arrays(src, tgt)
+    t0 = time.perf_counter()
+    wv, we = og.betweenness(threads=threads)
+    cpu_s = time.perf_counter() - t0
+    rel = max(float(np.abs(vb - wv).max() / max(np.abs(wv).max(), 1.0)),
+              float(np.abs(eb - we).max() / max(np.abs(we).max(), 1.0)))
+    work = float(n) * m
+    return {"workload": f"rmat{scale} (n={n}, m={m}), unweighted, every vertex a source",
+            "gpu_ms": gpu_ms, "gpu_call_ms": wall * 1e3, "gpu_gteps": work / (gpu_ms / 1e3) / 1e9,
+            "cpu_oracle_s": cpu_s, "cpu_cores": threads,
+            "cpu_gteps": work / cpu_s / 1e9, "speedup_vs_cpu": cpu_s / (wall if wall else 1.0),
+            "max_rel_diff_vs_oracle": rel}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -431,7 +477,7 @@ def main():
     ap.add_argument("--cpu-sweeps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--section", choices=["adjoint", "ppr_batch", "graph_batch"],
+    ap.add_argument("--section", choices=["adjoint", "ppr_batch", "graph_batch", "betweenness"],
                     help="run only this secondary measurement (adjoint on --workload's graph) "
                          "and print its JSON")
     ap.add_argument("--ppr-scale", type=int, default=22, help="R-MAT scale of the ppr_batch graph")
@@ -444,13 +490,15 @@ def main():
     import numpy as np
     import torch
 
-    if args.section in ("ppr_batch", "graph_batch"):
+    if args.section in ("ppr_batch", "graph_batch", "betweenness"):
         from graph_tool import _ffi
         device = torch.device("cuda", local)
         torch.cuda.set_device(device)
         stream = torch.cuda.current_stream(device)
         if args.section == "ppr_batch":
             out = ppr_section(_ffi.lib(), device, stream, B=args.ppr_b, scale=args.ppr_scale)
+        elif args.section == "betweenness":
+            out = betweenness_section(_ffi.lib(), device, stream)
         else:
             out = graph_batch_section(_ffi.lib(), device, stream, G=args.graphs)
         print(json.dumps({"section": args.section, **out}), flush=True)
@@ -619,7 +667,8 @@ def main():
     secondary = {}
     if not args.no_secondary and world == 1:
         for name, fn in (("adjoint", adjoint_section), ("ppr_batch", ppr_section),
-                         ("graph_batch", graph_batch_section)):
+                         ("graph_batch", graph_batch_section),
+                         ("betweenness", betweenness_section)):
             try:
                 secondary[name] = fn(L, h, n, m, device, stream, wl) if name == "adjoint" else fn(L, device, stream)
             except Exception as e:  # noqa: BLE001  (reported, the headline stands)
