@@ -740,9 +740,11 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         }
         // the gathered vectors carry one more entry, kept 0: the slices'
         // padding gathers it
+        // (a sweep does not store y of a dangling row: it stays 0, from the
+        // prime in y0 and from this clear in y1)
         DevBuf<float> r0(n, s), r1(n, s), y0((size_t)n + 1, s), y1((size_t)n + 1, s);
         GTC_CUDA(cudaMemsetAsync(y0.get() + n, 0, sizeof(float), s));
-        GTC_CUDA(cudaMemsetAsync(y1.get() + n, 0, sizeof(float), s));
+        GTC_CUDA(cudaMemsetAsync(y1.get(), 0, ((size_t)n + 1) * sizeof(float), s));
         if (n) {
             k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.x64.get(), GTC_F64, nullptr,
                                                               r0.get());

@@ -152,7 +152,9 @@ __device__ __forceinline__ void row_finish(const SweepArgs& A, uint32_t v, const
         const float r = __fadd_rn(__fmul_rn(psink, pv), sum);
         const float nv = __fadd_rn(__fmul_rn(A.one_minus_d, pv), __fmul_rn(A.d, r));
         __stcs(A.next + v, nv);
-        A.ynext[v] = __fmul_rn(nv, in.invdeg);
+        // y of a dangling row is 0 (invdeg 0) in both buffers already: not
+        // storing it keeps those lines out of L2
+        if (!in.sink) A.ynext[v] = __fmul_rn(nv, in.invdeg);
         ta = fabsf(__fsub_rn(nv, in.prev));
         tb = in.sink ? nv : 0.f;
     } else if (MODE == MODE_ADJOINT) {
@@ -223,15 +225,17 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
     for (uint32_t bk = gw; bk < n_buckets; bk += nw) {
     KahanLite bucket_a, bucket_b;
     // the next item's descriptor is loaded while this item runs
-    uint4 Unext = __ldg(A.units + bk);
+    // (the work list and the slices' row lists are read once a sweep:
+    // evict-first, like the index stream, so the gathered vector keeps L2)
+    uint4 Unext = __ldcs(A.units + bk);
     for (uint32_t u = bk; u < A.n_units; u += n_buckets) {
         const uint4 U = Unext;
-        if (u + n_buckets < A.n_units) Unext = __ldg(A.units + u + n_buckets);
+        if (u + n_buckets < A.n_units) Unext = __ldcs(A.units + u + n_buckets);
         if (U.x == UNIT_SLICES) {
             // {kind, slice, first entry, steps}: no table lookup before the
             // index stream starts
             const uint32_t k = U.y, b = U.z, len = U.w;
-            const uint32_t row = __ldg(A.slice_rows + 32 * k + lane);
+            const uint32_t row = __ldcs(A.slice_rows + 32 * k + lane);
             const uint32_t* ip = A.sidx + b + lane;
             const float* wp = WEIGHTED ? A.sw + b + lane : nullptr;
             KahanLite acc;
@@ -311,21 +315,33 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
             }
             KahanLite kl;
             uint32_t p = b + lane;
-            for (; p + 96 < e; p += 128) {
-                const uint32_t s0 = __ldcs(A.other + p), s1 = __ldcs(A.other + p + 32),
-                               s2 = __ldcs(A.other + p + 64), s3 = __ldcs(A.other + p + 96);
+            // rounds of four entries a lane; the next round's indices are
+            // loaded before this round's gathers (as in the slice loop)
+            auto round = [&](uint32_t q, uint32_t s0, uint32_t s1, uint32_t s2, uint32_t s3) {
                 float v0 = gather<HOT>(A, hot, s0), v1 = gather<HOT>(A, hot, s1);
                 float v2 = gather<HOT>(A, hot, s2), v3 = gather<HOT>(A, hot, s3);
                 if (WEIGHTED) {
-                    v0 = __fmul_rn(v0, __ldcs(A.w + p));
-                    v1 = __fmul_rn(v1, __ldcs(A.w + p + 32));
-                    v2 = __fmul_rn(v2, __ldcs(A.w + p + 64));
-                    v3 = __fmul_rn(v3, __ldcs(A.w + p + 96));
+                    v0 = __fmul_rn(v0, __ldcs(A.w + q));
+                    v1 = __fmul_rn(v1, __ldcs(A.w + q + 32));
+                    v2 = __fmul_rn(v2, __ldcs(A.w + q + 64));
+                    v3 = __fmul_rn(v3, __ldcs(A.w + q + 96));
                 }
                 kl.add(v0);
                 kl.add(v1);
                 kl.add(v2);
                 kl.add(v3);
+            };
+            if (p + 96 < e) {
+                uint32_t s0 = __ldcs(A.other + p), s1 = __ldcs(A.other + p + 32),
+                         s2 = __ldcs(A.other + p + 64), s3 = __ldcs(A.other + p + 96);
+                for (; p + 128 + 96 < e; p += 128) {
+                    const uint32_t n0 = __ldcs(A.other + p + 128), n1 = __ldcs(A.other + p + 160),
+                                   n2 = __ldcs(A.other + p + 192), n3 = __ldcs(A.other + p + 224);
+                    round(p, s0, s1, s2, s3);
+                    s0 = n0, s1 = n1, s2 = n2, s3 = n3;
+                }
+                round(p, s0, s1, s2, s3);
+                p += 128;
             }
             for (; p < e; p += 32) {
                 float v = gather<HOT>(A, hot, __ldcs(A.other + p));
