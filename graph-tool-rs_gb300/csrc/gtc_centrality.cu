@@ -435,8 +435,22 @@ inline uint32_t hot_entries(uint32_t n) {
     return h & ~3u;
 }
 
-// The kernel variants the autotuner chooses between.
-enum SweepVariant { VAR_L1 = 0, VAR_HOT = 1, N_VARIANTS = 2 };
+// The kernel variants the autotuner chooses between.  They compute
+// bit-identical results (the same per-item order and fold); they differ in
+// where the gathers of the hottest entries are served:
+//   VAR_L1     256-thread CTAs, 6 per SM, every gather through L1/L2
+//   VAR_HOT    one 1024-thread CTA per SM, the first 32,768 entries of the
+//              gathered vector (labels follow out-degree, so the most
+//              gathered ones) in its shared memory
+//   VAR_HOT24  the same kernel with 24,576,
+//   VAR_HOT16  16,384
+//   VAR_HOT8   and 8,192 hot entries: less shared memory leaves more of the
+//              SM's L1 to the gathers in flight, which can matter more than
+//              the entries given up (it does on the R-MAT and Chung-Lu
+//              graphs measured)
+enum SweepVariant {
+    VAR_L1 = 0, VAR_HOT = 1, VAR_HOT24 = 2, VAR_HOT16 = 3, VAR_HOT8 = 4, N_VARIANTS = 5
+};
 
 struct VariantShape {
     unsigned grid, threads;
@@ -467,14 +481,24 @@ VariantShape variant_shape(uint32_t n_units, uint32_t hot_n) {
     return v;
 }
 
+inline uint32_t variant_hot_cap(int var) {
+    return var == VAR_HOT ? (uint32_t)SP_HOT
+         : var == VAR_HOT24 ? 24576u
+         : var == VAR_HOT16 ? 16384u
+         : 8192u;
+}
+
 template <int MODE, bool W>
 void launch_variant(int var, const SweepArgs& A, cudaStream_t s) {
-    if (var == VAR_HOT) {
-        VariantShape v = variant_shape<MODE, W, 1024, true>(A.n_units, A.hot_n);
-        k_sweep<MODE, W, 1024, true><<<v.grid, v.threads, v.smem, s>>>(A);
-    } else {
+    if (var == VAR_L1) {
         VariantShape v = variant_shape<MODE, W, 256, false>(A.n_units, A.hot_n);
         k_sweep<MODE, W, 256, false><<<v.grid, v.threads, v.smem, s>>>(A);
+    } else {
+        SweepArgs B = A;
+        const uint32_t cap = variant_hot_cap(var);
+        B.hot_n = (A.hot_n < cap ? A.hot_n : cap) & ~3u;
+        VariantShape v = variant_shape<MODE, W, 1024, true>(B.n_units, B.hot_n);
+        k_sweep<MODE, W, 1024, true><<<v.grid, v.threads, v.smem, s>>>(B);
     }
     GTC_LAUNCHED();
 }
@@ -497,7 +521,11 @@ int tuned_variant(Units& u, const SweepArgs& A, bool weighted, cudaStream_t s, u
     int& v = u.variant[MODE][weighted ? 1 : 0];
     if (v >= 0) return v;
     if (const char* e = std::getenv("GTC_SWEEP_VARIANT")) {  // pinned for experiments
-        v = std::atoi(e) == 1 ? VAR_HOT : VAR_L1;
+        // 0 L1, 1 HOT, 3 HOT24, 4 HOT16, 5 HOT8 (2 is the segmented sweep,
+        // chosen elsewhere)
+        const int k = std::atoi(e);
+        v = k == 1 ? VAR_HOT : k == 3 ? VAR_HOT24 : k == 4 ? VAR_HOT16 : k == 5 ? VAR_HOT8
+          : VAR_L1;
         return v;
     }
     cudaEvent_t e0, e1;
