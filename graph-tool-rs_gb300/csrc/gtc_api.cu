@@ -317,6 +317,18 @@ int gtc_pagerank(gtc_graph* g, const gtc_view* view, const double* weight, uint6
     });
 }
 
+int gtc_weighted_degree(gtc_graph* g, const gtc_view* view, int32_t in_edges, const double* weight,
+                        uint64_t weight_len, double* deg, uint64_t deg_len, const gtc_options* opt) {
+    return guarded([&] {
+        GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
+        GTC_REQUIRE(!weight || weight_len >= g->m, GTC_ERR_ARG,
+                    "weight map is shorter than the edge bound");
+        GTC_REQUIRE(deg || g->n == 0, GTC_ERR_ARG, "deg is NULL");
+        GTC_REQUIRE(deg_len >= g->n, GTC_ERR_ARG, "degree map is shorter than the vertex bound");
+        gtc::weighted_degree(g, view, weight, in_edges != 0, deg, stream_of(g, opt));
+    });
+}
+
 int gtc_betweenness(gtc_graph* g, const gtc_view* view, int32_t undirected, double* vertex_bc,
                     uint64_t vertex_len, double* edge_bc, uint64_t edge_len,
                     const gtc_options* opt, gtc_result* result) {

@@ -1263,4 +1263,40 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     g->launches += L;
 }
 
+// weighted_out_degree / weighted_in_degree (crates/gt-algo/src/degree.rs
+// :122-160) of every vertex of a view: the FP64 left fold from 0.0 of the
+// weights over the out-half (in-half) in storage order -- the reference's
+// sum_weights (degree.rs:68-82) -- or the degree for a Unity map (weight
+// NULL).  Vertices outside the view get 0.  Host arrays.
+void weighted_degree(gtc_graph* g, const gtc_view* vw, const double* w_host, bool in_dir,
+                     double* deg_host, cudaStream_t s) {
+    uint64_t L = 0;
+    View view;
+    view.prepare(g, vw, s, &L);
+    const uint32_t n = view.n;
+    const uint64_t m = g->m;
+    DevBuf<double> dw;
+    if (w_host && m) {
+        dw.alloc(m, s);
+        GTC_CUDA(cudaMemcpyAsync(dw.get(), w_host, m * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    if (n) {
+        DevBuf<double> deg(n, s), out(n, s);
+        DevBuf<uint8_t> sink(n, s);
+        k_degree<<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(
+            n, in_dir ? view.pull_off : view.push_off, in_dir ? view.pull_eid : view.push_eid,
+            w_host ? dw.get() : nullptr, GTC_F64, view.active_or_null(), deg.get(), sink.get());
+        GTC_LAUNCHED();
+        k_store<double><<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, g->iperm.get(), deg.get(),
+                                                                   nullptr, nullptr, out.get(),
+                                                                   GTC_F64);
+        GTC_LAUNCHED();
+        L += 2;
+        GTC_CUDA(cudaMemcpyAsync(deg_host, out.get(), (size_t)n * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+    }
+    GTC_CUDA(cudaStreamSynchronize(s));
+    g->launches += L;
+}
+
 }  // namespace gtc

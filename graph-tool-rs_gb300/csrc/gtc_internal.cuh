@@ -353,6 +353,9 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
 // solves (gtc_centrality.cu)
 void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc_result* res,
                       cudaStream_t s);
+// Weighted out- or in-degree of every vertex of a view (host arrays).
+void weighted_degree(gtc_graph* g, const gtc_view* vw, const double* w_host, bool in_dir,
+                     double* deg_host, cudaStream_t s);
 // Brandes betweenness of a view (gtc_betweenness.cu); host output arrays
 // (vertex bound / edge bound entries), either may be null.
 void betweenness(gtc_graph* g, const gtc_view* vw, bool undirected, double* vb_host,

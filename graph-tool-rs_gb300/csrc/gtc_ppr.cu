@@ -944,6 +944,13 @@ inline uint32_t ppr_lines(uint32_t active) {
     return c <= 4 ? c : (c <= 6 ? 6 : (c + 3) / 4 * 4);
 }
 
+// GTC_PPR_HANDOFF=k overrides the column count at which the batch hands its
+// last columns to the single-vector solver (for measurements).
+uint32_t ppr_handoff() {
+    const char* e = std::getenv("GTC_PPR_HANDOFF");
+    return e ? (uint32_t)std::atoi(e) : PPR_HANDOFF;
+}
+
 // GTC_PPR_VARIANT=regs|bulk pins the gather variant (default bulk).
 int ppr_variant() {
     const char* e = std::getenv("GTC_PPR_VARIANT");
@@ -1117,6 +1124,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     float *zc = z0.get(), *zx = z1.get();
     PprTimer total(s), tsw(s);
     total.start();
+    const uint32_t handoff = ppr_handoff();
     while (running > 0) {
         // the output layout: the columns still running, packed
         out_slot.assign(s_in, PPR_NONE);
@@ -1187,7 +1195,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
         s_in = s_out;
         C = c_out;
         std::swap(zc, zx);
-        if (running > 0 && running <= PPR_HANDOFF && n) {
+        if (running > 0 && running <= handoff && n) {
             // the last few columns: their iterates to the output, then the
             // single-vector solver continues each from there (pagerank_with
             // from a warm start is the same iteration)

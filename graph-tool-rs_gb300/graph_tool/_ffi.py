@@ -125,6 +125,8 @@ SIGNATURES = {
     "gtc_pagerank_noalloc": (C.c_int, [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_double, C.c_double, C.c_uint64, C.c_void_p,
                                        C.POINTER(C.c_uint64), C.c_void_p]),
+    "gtc_weighted_degree": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_int32, f64p, C.c_uint64,
+                                      f64p, C.c_uint64, C.POINTER(Options)]),
     "gtc_betweenness": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_int32, f64p, C.c_uint64, f64p,
                                   C.c_uint64, C.POINTER(Options), C.POINTER(Result)]),
     "gtc_gt_open": (C.c_int, [C.c_char_p, C.c_uint64, C.POINTER(C.c_void_p)]),

@@ -266,6 +266,27 @@ class Graph:
                    vfilt, efilt, precision, stream, True, plan_len)
         return r if result else (r.eigenvalue, r.iterations)
 
+    def weighted_degree(self, weight: PropertyMap | None = None, direction: str = "out",
+                        reversed: bool = False, vfilt=None, efilt=None) -> PropertyMap:
+        """weighted_out_degree / weighted_in_degree (crates/gt-algo/src/degree.rs
+        :122-160) of every vertex: the FP64 left fold of the weights over its
+        out-edges (``direction="out"``) or in-edges (``"in"``) in storage
+        order; ``weight=None`` is Unity (the degree)."""
+        if direction not in ("out", "in"):
+            raise ValueError("direction must be 'out' or 'in'")
+        w = _f64_map(self, weight, "e", "weight")
+        out = self.new_vertex_property("double")
+        d = out.sized_for()
+        vm = _mask(self, vfilt, self.num_vertices())
+        em = _mask(self, efilt, self.edge_index_range())
+        view = _ffi.View(int(bool(reversed)), 0, _ffi.ptr(vm, _ffi.u8p),
+                         0 if vm is None else vm.size, _ffi.ptr(em, _ffi.u8p),
+                         0 if em is None else em.size)
+        _ffi.check(_ffi.lib().gtc_weighted_degree(
+            self.handle(), C.byref(view), int(direction == "in"), _ffi.ptr(w, _ffi.f64p),
+            0 if w is None else w.size, _ffi.ptr(d, _ffi.f64p), d.size, None))
+        return out
+
     def betweenness(self, vertex_bc: PropertyMap | None = None,
                     edge_bc: PropertyMap | None = None, undirected: bool = False,
                     reversed: bool = False, vfilt=None, efilt=None, result: bool = False):

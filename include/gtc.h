@@ -244,6 +244,17 @@ int gtc_eigenvector(gtc_graph* g, const gtc_view* view, const double* weight,
                     uint64_t weight_len, const gtc_power_iteration* params, double* x,
                     uint64_t x_len, uint64_t x_had, const gtc_options* opt, gtc_result* result);
 
+/* weighted_out_degree (in_edges == 0) and weighted_in_degree (in_edges != 0),
+ * crates/gt-algo/src/degree.rs:122-160, of every vertex of the view: the
+ * FP64 sum of the weight map over the vertex's out-half (in-half) in storage
+ * order, as a left fold from 0.0 (sum_weights, degree.rs:68-82), so the
+ * result is bit-identical to the reference's; weight == NULL is Unity (the
+ * degree).  The degree pass of pagerank (centrality.rs:281-297) is this fold
+ * over the out-half.  deg: vertex bound entries, by vertex index; 0 for a
+ * vertex outside the view.  Host arrays. */
+int gtc_weighted_degree(gtc_graph* g, const gtc_view* view, int32_t in_edges, const double* weight,
+                        uint64_t weight_len, double* deg, uint64_t deg_len, const gtc_options* opt);
+
 /* Betweenness centrality (Brandes), crates/gt-algo/src/centrality.rs:633-689:
  * unweighted, every vertex of the view a source, unnormalised.  Both maps are
  * overwritten (init_centrality_map): vertex_bc by vertex index (vertex_len >=
