@@ -653,6 +653,7 @@ def main():
 
     # ---- CPU baseline ------------------------------------------------------
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu:
         src_np = src.cpu().numpy().astype(np.uint32)
         tgt_np = tgt.cpu().numpy().astype(np.uint32)
@@ -662,6 +663,20 @@ def main():
         cpu = {"value": v, "unit": "GTEPS", "cores": threads, "kind": "port",
                "sample": f"{it} sweeps of the same graph (n={n}, m={m}) by gtc_oracle.c, "
                          f"{threads} OpenMP threads, {dt:.2f} s"}
+        # full-size parity: the oracle's complete f64 solve of this graph against
+        # the last device solve (FP32), outside every timed region
+        try:
+            t0 = time.perf_counter()
+            want, it_o = g.pagerank(weight=w_cpu, damping=DAMPING, epsilon=wl["eps"],
+                                    max_iter=MAX_ITER, grain=4096, threads=threads)
+            got = rank_t.double().cpu().numpy()
+            diff = np.abs(got - want)
+            parity = {"rel_l1": float(diff.sum() / np.abs(want).sum()),
+                      "max_abs": float(diff.max()), "sweeps_gpu": iters_per_solve,
+                      "sweeps_oracle": int(it_o), "oracle_s": time.perf_counter() - t0,
+                      "reference": "gtc_oracle.c f64 pagerank, same graph, same epsilon"}
+        except Exception as e:  # noqa: BLE001  (reported; the headline stands)
+            parity = {"error": repr(e)}
         del g
 
     secondary = {}
@@ -684,7 +699,7 @@ def main():
                 "workload": args.workload, "graph": wl["label"], "n": n, "m": m,
                 "damping": DAMPING, "epsilon": wl["eps"], "sweeps_per_solve": iters_per_solve,
                 "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "parity_vs_f64_oracle": parity,
             "gpu_launches": int(launches), "sweep_launches": int(sweep_launches),
             "clocks": clk.summary(),
         }
