@@ -90,6 +90,24 @@ def env_rank():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def max_over_ranks(t_ms: float, world: int) -> float:
+    """The slowest rank's timed region (every rank calls this; the process
+    group is gloo, so the reduction runs on the host)."""
+    if world <= 1:
+        return t_ms
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([t_ms], dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def whole_job_gteps(world: int, m: int, sweeps: int, t_ms: float) -> float:
+    """Every rank solves its own replica of the graph (weak scaling): the
+    edge-sweeps of all ranks over the slowest rank's time."""
+    return world * m * sweeps / (t_ms / 1e3) / 1e9
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -596,12 +614,8 @@ def main():
             sweep_launches += r.sweep_launches
         e1.record(stream)
         torch.cuda.synchronize()
-    t_ms = e0.elapsed_time(e1)
-    if world > 1:
-        tt = torch.tensor([t_ms], dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(tt.item())
-    value = world * m * sweeps / (t_ms / 1e3) / 1e9
+    t_ms = max_over_ranks(e0.elapsed_time(e1), world)
+    value = whole_job_gteps(world, m, sweeps, t_ms)
     iters_per_solve = sweeps / args.steps
 
     # ---- e2e through the host-buffer C ABI ------------------------------
