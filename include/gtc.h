@@ -8,6 +8,15 @@
  *   gtc_pagerank     pagerank / pagerank_with    crates/gt-algo/src/centrality.rs:234-248, 261-384
  *   gtc_eigenvector  eigenvector                 crates/gt-algo/src/centrality.rs:405-497
  *
+ * and, around that path:
+ *
+ *   gtc_betweenness      betweenness                crates/gt-algo/src/centrality.rs:633-689
+ *   gtc_weighted_degree  weighted_out/in_degree     crates/gt-algo/src/degree.rs:122-160
+ *   gtc_gt_*             gt_io::gt::read            crates/gt-io/src/gt.rs:555-820
+ *   gtc_ppr_batch, gtc_graph_batch_*, gtc_pagerank_batch, gtc_pagerank_adjoint,
+ *   gtc_pagerank_noalloc (no counterparts: batched, many-graph, gradient and
+ *   allocation-free forms of pagerank)
+ *
  * and the graph they run over is the reference's adjacency storage,
  * crates/gt-core/src/adj/list.rs:67-79 (AdjList) with its per-vertex blocks
  * crates/gt-core/src/adj/block.rs:54-57: a handle built by replaying
