@@ -3,8 +3,8 @@
 * GTC_PREC_F64_EXACT: bit-identical results and sweep counts (the
   reference's arithmetic and fold order, same Plan).
 * GTC_PREC_F32: the reference's known answers to FP32 accuracy, and
-  relative L1 error <= 1e-6 against the oracle's f64 result (the north-star
-  tolerance), with both sweep counts reported.
+  relative L1 error <= 1e-6 against the oracle's f64 result (the tolerance
+  this FP32 path is held to), with both sweep counts reported.
 """
 import numpy as np
 import pytest
