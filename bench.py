@@ -677,6 +677,12 @@ def main():
         cpu = {"value": v, "unit": "GTEPS", "cores": threads, "kind": "port",
                "sample": f"{it} sweeps of the same graph (n={n}, m={m}) by gtc_oracle.c, "
                          f"{threads} OpenMP threads, {dt:.2f} s"}
+        try:  # the same sample on one core
+            v1, dt1, _ = run_cpu(g, m, w_cpu, wl["eps"], args.cpu_sweeps, 1)
+            cpu["value_1_core"] = v1
+            cpu["seconds_1_core"] = dt1
+        except Exception as e:  # noqa: BLE001
+            cpu["value_1_core"] = {"error": repr(e)}
         # full-size parity: the oracle's complete f64 solve of this graph against
         # the last device solve (FP32), outside every timed region
         try:
