@@ -234,7 +234,9 @@ void parse(gtc_gt_file& f) {
         const int w = scalar_width(kind);
         uint64_t tmp = 0;
         if (kind <= K_LONG_DOUBLE) {
-            if (P.count > (c.len - c.pos) / (uint64_t)w) c.need(P.count * (uint64_t)w);
+            if (P.count > (c.len - c.pos) / (uint64_t)w)
+                throw Error{GTC_ERR_ARG, at_byte(c.pos, "unexpected end of file, wanted " +
+                                                            std::to_string(P.count) + " values")};
             c.pos += P.count * (uint64_t)w;
         } else if (kind == K_STR) {
             for (uint64_t j = 0; j < P.count; ++j) c.text(&tmp, "", false, P.name);
@@ -248,7 +250,11 @@ void parse(gtc_gt_file& f) {
         } else {  // vectors of fixed-width elements
             for (uint64_t j = 0; j < P.count; ++j) {
                 const uint64_t k = c.u64();
-                if (k > (c.len - c.pos) / (uint64_t)w) c.need(k * (uint64_t)w);
+                // compared before multiplying: a declared count near 2^64
+                // would wrap k * w around to a small length
+                if (k > (c.len - c.pos) / (uint64_t)w)
+                    throw Error{GTC_ERR_ARG, at_byte(c.pos, "unexpected end of file, a vector of " +
+                                                                std::to_string(k) + " elements")};
                 c.pos += k * (uint64_t)w;
             }
         }

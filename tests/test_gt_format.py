@@ -279,6 +279,16 @@ def test_absurd_declared_lengths_do_not_allocate(gtc):
     assert "declares" in _refused(bytes(b))
 
 
+def test_a_vector_count_that_would_wrap_is_refused(gtc):
+    # a vector<double> value declaring 2^61 + 1 elements: 8 x that count wraps
+    # around 2^64 to 8, which must not pass for a short remainder
+    b = bytearray(G.write(1, [], True, [("v", G.VERTEX, 11, [[1.5]])]))
+    at = len(b) - 8 - 8  # the element count, then the one element
+    assert struct.unpack("<Q", b[at:at + 8])[0] == 1
+    b[at:at + 8] = struct.pack("<Q", (1 << 61) + 1)
+    assert "unexpected end of file" in _refused(bytes(b))
+
+
 def test_out_of_range_index_is_left_to_the_device_check(gtc):
     # the framing is sound, so the host parse accepts it; gtc_gt_graph (on
     # the GPU) refuses the index -- the oracle refuses it while reading
