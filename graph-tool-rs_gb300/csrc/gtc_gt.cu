@@ -191,6 +191,12 @@ void parse(gtc_gt_file& f) {
     f.n = c.u64();
     if (f.n > 0 && f.n - 1 > 0xFFFFFFFEull)
         throw Error{GTC_ERR_ARG, "the document's vertex count exceeds the index space"};
+    // every vertex record holds at least its 8-byte count: a document too
+    // short for N of them is truncated, and nothing is sized from N first
+    if (f.n > (c.len - c.pos) / 8)
+        throw Error{GTC_ERR_ARG, at_byte(c.pos, "unexpected end of file, " + std::to_string(f.n) +
+                                                    " vertex records need at least " +
+                                                    std::to_string(f.n) + " x 8 bytes")};
     f.width = vint_width(f.n);
     f.list_at.resize((size_t)f.n);
     f.e_off.resize((size_t)f.n + 1);

@@ -279,6 +279,19 @@ def test_absurd_declared_lengths_do_not_allocate(gtc):
     assert "declares" in _refused(bytes(b))
 
 
+def test_an_absurd_vertex_count_is_refused_before_anything_is_sized(gtc):
+    # u27_gt.rs:876-885: N = 2^40 is past the index space; N = 2^32 - 1 is
+    # inside it but the document cannot hold that many records
+    for n in ((1 << 40), (1 << 32) - 1):
+        b = bytearray(G.MAGIC) + bytes([G.VERSION, 0]) + struct.pack("<Q", 0) + bytes([1])
+        b += struct.pack("<Q", n)
+        msg = _refused(bytes(b))
+        assert "index space" in msg or "unexpected end of file" in msg, msg
+        with pytest.raises(G.GtError) as e:
+            G.read(bytes(b))
+        assert e.value.kind in ("Parse", "IndexWidthExceeded")
+
+
 def test_a_vector_count_that_would_wrap_is_refused(gtc):
     # a vector<double> value declaring 2^61 + 1 elements: 8 x that count wraps
     # around 2^64 to 8, which must not pass for a short remainder
