@@ -166,6 +166,55 @@ def test_library_parses_every_kind_in_both_byte_orders(gtc, n, big):
     _check_library_against_oracle(gtc, b)
 
 
+@pytest.mark.parametrize("n,width", [(1, 1), (255, 1), (256, 2), (65_535, 2), (65_536, 4)])
+def test_the_index_width_switches_at_the_boundaries(gtc, n, width):
+    # u27_gt.rs:250-286: the narrowest unsigned width holding N (N <= 255 is
+    # one byte); one edge 0 -> n-1
+    from graph_tool import gt as L
+    b = G.write(n, [(0, n - 1)], True)
+    clen = struct.unpack("<Q", b[8:16])[0]
+    lst = 16 + clen + 1 + 8
+    assert struct.unpack("<Q", b[lst:lst + 8])[0] == 1
+    assert int.from_bytes(b[lst + 8:lst + 8 + width], "little") == n - 1
+    assert len(b) == lst + 8 + width + 8 * (n - 1) + 8  # the other lists are empty, then nprops
+    f = L.GtFile(b)
+    assert (f.n, f.m) == (n, 1)
+    d = G.read(b)
+    assert (d["src"], d["tgt"]) == ([0], [n - 1])
+
+
+def test_empty_and_edgeless_documents_with_a_graph_property(gtc):
+    # u27_gt.rs:1072-1102
+    from graph_tool import gt as L
+    f = L.GtFile(G.write(0, [], False))
+    assert (f.n, f.m, f.directed, f.nprops) == (0, 0, False, 0)
+    f = L.GtFile(G.write(4, [], True, [("name", G.GRAPH, 6, ["four dots"])]))
+    assert (f.n, f.m, f.nprops) == (4, 0, 1)
+    assert f.properties() == [("name", G.GRAPH, 6, 1)]
+    assert f.values(0) == ["four dots"]
+
+
+def test_an_undirected_document_lists_each_edge_once(gtc):
+    # u27_gt.rs:1104-1120: the flag is metadata; the lists are the directed
+    # adjacency, one entry per edge
+    from graph_tool import gt as L
+    f = L.GtFile(G.write(2, [(0, 1)], False))
+    assert (f.n, f.m, f.directed) == (2, 1, False)
+
+
+@needs_ref
+def test_the_edge_column_of_lesmis_stays_with_its_edge(gtc):
+    # u27_gt.rs:547-590: the first list entry is 1 -> 0 with weight 1; the
+    # column is keyed by edge id, which is file order
+    from graph_tool import gt as L
+    f = L.GtFile(_fixture("lesmis.gt"))
+    names = [p[0] for p in f.properties()]
+    w = f.values(names.index("value"))
+    assert w.dtype == np.float64 and w.size == 254 and w[0] == 1.0
+    d = G.read(_fixture("lesmis.gt"))
+    assert np.array_equal(w, np.asarray(d["props"][4][3]))
+
+
 def test_big_endian_twin_reads_the_same(gtc):
     from graph_tool import gt as L
     le, *_ = _all_kinds_doc(7, False)
