@@ -42,8 +42,10 @@ More measurements ride on the same line (skipped with --no-secondary):
   betweenness  Brandes from every vertex of an R-MAT scale-14 graph (edge
             factor 16, deduplicated): GPU time against the CPU oracle on all
             host threads, edges x sources per second, and their difference.
+  eigenvector  eigenvector centrality on the weighted Chung-Lu graph,
+            epsilon 1e-7, max_iter 500: time, sweeps, eigenvalue, roofline.
 
-``--section adjoint|ppr_batch|graph_batch|betweenness`` runs one of them alone and prints
+``--section adjoint|ppr_batch|graph_batch|betweenness|eigenvector`` runs one of them alone and prints
 its JSON (``--ppr-scale``, ``--ppr-b``, ``--graphs`` shrink the last two for
 profiling; ``--workload`` picks the adjoint's graph).
 
@@ -442,6 +444,56 @@ def graph_batch_section(L, device, stream, G=4096):
             "cuda_graph_launches_per_solve": 1}
 
 
+def eigenvector_section(L, device, stream):
+    """Eigenvector centrality (centrality.rs:405-497 of graph-tool-rs) on the
+    Chung-Lu graph (n = 4,194,304, m ~ 67M, FP32 weights U(0.1, 1)), epsilon
+    1e-7, max_iter 500: time per solve and per sweep, the sweep count, the
+    eigenvalue, and the sweep kernel against the HBM roofline
+    (B_ev = 4(n+1) + 8m + 12n bytes a sweep)."""
+    import torch
+    from graph_tool import _ffi
+    wl = WORKLOADS["chunglu"]
+    n, src, tgt, w = make_graph(wl, device, 0)
+    m = int(src.numel())
+    h = C.c_void_p()
+    _ffi.check(L.gtc_graph_create_device(n, m, C.c_void_p(src.data_ptr()),
+                                         C.c_void_p(tgt.data_ptr()),
+                                         C.c_void_p(stream.cuda_stream), C.byref(h)))
+    try:
+        _ffi.check(L.gtc_graph_set_stream(h, C.c_void_p(stream.cuda_stream)))
+        del src, tgt
+        wv = _ffi.DVec.of(w)
+        x = torch.empty(n, dtype=torch.float32, device=device)
+        xv = _ffi.DVec.of(x)
+        params = _ffi.PowerIteration(1e-7, 500, n, (n + 4095) // 4096)
+        opt = _ffi.Options(_ffi.GTC_PREC_F32, 0, C.c_void_p(stream.cuda_stream), 1, 0)
+        runs = []
+
+        def solve():
+            r = _ffi.Result()
+            _ffi.check(L.gtc_eigenvector_device(h, None, C.byref(wv), C.byref(params),
+                                                C.byref(xv), 0, C.byref(opt), C.byref(r)))
+            runs.append(r)
+            return r
+
+        solve()
+        solve()  # the autotuner's trials, then a warm solve
+        runs.clear()
+        t_ms, _ = _events_ms(solve, stream, 3)
+        sweeps = sum(int(r.iterations) for r in runs)
+        sweep_s = sum(r.sweep_ms for r in runs) / 1e3 / max(sweeps, 1)
+        peak, peak_kind = measured_peaks()
+        b_ev = 4 * (n + 1) + 8 * m + 12 * n
+        return {"workload": "Chung-Lu n=4,194,304, m~67M, FP32 weights U(0.1,1), eps 1e-7, "
+                            "max_iter 500",
+                "n": n, "m": m, "solve_ms": t_ms, "sweeps": int(runs[-1].iterations),
+                "eigenvalue": float(runs[-1].eigenvalue), "ms_per_sweep": sweep_s * 1e3,
+                "gteps": m * sweeps / 3 / (t_ms / 1e3) / 1e9,
+                "roofline_frac": b_ev / sweep_s / 1e9 / peak, "peak_kind": peak_kind}
+    finally:
+        L.gtc_graph_destroy(h)
+
+
 def betweenness_section(L, device, stream, scale=14):
     """Betweenness (Brandes, every vertex a source) of an R-MAT graph
     (edge factor 16, deduplicated): the GPU (gtc_betweenness, host maps) and
@@ -495,7 +547,8 @@ def main():
     ap.add_argument("--cpu-sweeps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--section", choices=["adjoint", "ppr_batch", "graph_batch", "betweenness"],
+    ap.add_argument("--section", choices=["adjoint", "ppr_batch", "graph_batch", "betweenness",
+                                          "eigenvector"],
                     help="run only this secondary measurement (adjoint on --workload's graph) "
                          "and print its JSON")
     ap.add_argument("--ppr-scale", type=int, default=22, help="R-MAT scale of the ppr_batch graph")
@@ -508,7 +561,7 @@ def main():
     import numpy as np
     import torch
 
-    if args.section in ("ppr_batch", "graph_batch", "betweenness"):
+    if args.section in ("ppr_batch", "graph_batch", "betweenness", "eigenvector"):
         from graph_tool import _ffi
         device = torch.device("cuda", local)
         torch.cuda.set_device(device)
@@ -517,6 +570,8 @@ def main():
             out = ppr_section(_ffi.lib(), device, stream, B=args.ppr_b, scale=args.ppr_scale)
         elif args.section == "betweenness":
             out = betweenness_section(_ffi.lib(), device, stream)
+        elif args.section == "eigenvector":
+            out = eigenvector_section(_ffi.lib(), device, stream)
         else:
             out = graph_batch_section(_ffi.lib(), device, stream, G=args.graphs)
         print(json.dumps({"section": args.section, **out}), flush=True)
@@ -703,7 +758,8 @@ def main():
     if not args.no_secondary and world == 1:
         for name, fn in (("adjoint", adjoint_section), ("ppr_batch", ppr_section),
                          ("graph_batch", graph_batch_section),
-                         ("betweenness", betweenness_section)):
+                         ("betweenness", betweenness_section),
+                         ("eigenvector", eigenvector_section)):
             try:
                 secondary[name] = fn(L, h, n, m, device, stream, wl) if name == "adjoint" else fn(L, device, stream)
             except Exception as e:  # noqa: BLE001  (reported, the headline stands)
