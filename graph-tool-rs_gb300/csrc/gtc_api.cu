@@ -46,6 +46,18 @@ void require_device() {
     }
 }
 
+int sm_count() {
+    static int cached[64] = {};
+    int dev = 0;
+    GTC_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && cached[dev]) return cached[dev];
+    int sms = 0;
+    GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (sms < 1) sms = 1;
+    if (dev >= 0 && dev < 64) cached[dev] = sms;
+    return sms;
+}
+
 template <class F>
 static int guarded(F&& f) {
     try {
@@ -117,6 +129,11 @@ static void check_params(const gtc_graph* g, const gtc_power_iteration* p, gtc_p
     GTC_REQUIRE(out.plan_chunks <= (out.plan_len ? out.plan_len : 1), GTC_ERR_ARG,
                 "plan has more chunks than items");
     GTC_REQUIRE(!std::isnan(out.epsilon), GTC_ERR_ARG, "epsilon is NaN");
+    // The sweeps stop at the first L1 change below epsilon or at max_iter.
+    // An L1 change is never negative, so without a cap epsilon <= 0 would
+    // never stop (the reference's loop would spin forever); refused here.
+    GTC_REQUIRE(out.max_iter != 0 || out.epsilon > 0.0, GTC_ERR_ARG,
+                "max_iter = 0 (uncapped) with epsilon <= 0 would never stop");
 }
 
 }  // namespace gtc
@@ -240,9 +257,12 @@ static cudaStream_t stream_of(const gtc_graph* g, const gtc_options* opt) {
 
 static void common_opts(const gtc_options* opt, SolveIn& in) {
     in.precision = opt ? opt->precision : GTC_PREC_F32;
+    in.schedule = opt ? opt->schedule : GTC_SCHED_AUTO;
     in.timing = opt && opt->timing;
     GTC_REQUIRE(in.precision == GTC_PREC_F32 || in.precision == GTC_PREC_F64_EXACT, GTC_ERR_ARG,
                 "unknown precision");
+    GTC_REQUIRE(in.schedule >= GTC_SCHED_AUTO && in.schedule <= GTC_SCHED_HOT8K, GTC_ERR_ARG,
+                "unknown schedule");
 }
 
 static DVec dvec_in(const gtc_dvec* v, uint64_t need, const char* what) {
@@ -524,6 +544,9 @@ int gtc_ppr_batch_device(gtc_graph* g, const gtc_view* view, const gtc_dvec* wei
         in.out_dtype = ranks->dtype;
         in.iters = iters;
         in.timing = opt && opt->timing;
+        in.gather = opt ? opt->ppr_gather : GTC_PPR_BULK;
+        GTC_REQUIRE(in.gather == GTC_PPR_BULK || in.gather == GTC_PPR_REGS, GTC_ERR_ARG,
+                    "unknown ppr_gather");
         gtc_result r{};
         gtc::ppr_batch(g, view, in, &r, stream_of(g, opt));
         if (result) *result = r;

@@ -220,7 +220,7 @@ void betweenness(gtc_graph* g, const gtc_view* vw, bool undirected, double* vb_h
     size_t free_b = 0, total_b = 0;
     GTC_CUDA(cudaMemGetInfo(&free_b, &total_b));
     const uint64_t budget = std::max<uint64_t>(free_b / 4, per_cta);
-    uint64_t G = std::min<uint64_t>({(uint64_t)2 * kSMs, std::max<uint32_t>(nsrc, 1u),
+    uint64_t G = std::min<uint64_t>({(uint64_t)2 * sm_count(), std::max<uint32_t>(nsrc, 1u),
                                      budget / per_cta});
     G = std::max<uint64_t>(G, 1);
     DevBuf<int> dist(G * n, s);

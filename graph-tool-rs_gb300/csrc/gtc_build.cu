@@ -429,7 +429,7 @@ static void relabel_half(uint32_t n, uint32_t m, const uint32_t* perm, const uin
     }
     scan_exclusive_u32(deg.get(), nh.off.get(), n, s, L);
     if (n && m) {
-        k_permute_rows<<<kSMs * 16, TB, 0, s>>>(n, perm, iperm, h.off.get(), h.eid.get(), endpoint,
+        k_permute_rows<<<sm_count() * 16, TB, 0, s>>>(n, perm, iperm, h.off.get(), h.eid.get(), endpoint,
                                                nh.off.get(), nh.eid.get(), nh.other.get());
         GTC_LAUNCHED();
         *L += 1;

@@ -407,9 +407,9 @@ struct FoldBufs {
 };
 
 unsigned persistent_blocks(uint32_t rows) {
-    // one row per warp, at most 152 SMs x 8 resident blocks of 256 threads
+    // one row per warp, at most 8 resident blocks of 256 threads per SM
     unsigned want = (rows + (PR_NT / 32) - 1) / (PR_NT / 32);
-    unsigned cap = kSMs * 8;
+    unsigned cap = (unsigned)sm_count() * 8;
     return want < 1 ? 1 : (want > cap ? cap : want);
 }
 
@@ -517,36 +517,31 @@ void launch_sweep(int var, const SweepArgs& A, bool weighted, cudaStream_t s) {
 // graph.  The variants compute bit-identical results (same per-item order and
 // fold), so the choice changes speed only.
 template <int MODE>
-int tuned_variant(Units& u, const SweepArgs& A, bool weighted, cudaStream_t s, uint64_t* L) {
+int tuned_variant(Units& u, const SweepArgs& A, bool weighted, int schedule, cudaStream_t s,
+                  uint64_t* L) {
+    switch (schedule) {  // a pinned kernel (gtc_schedule)
+        case GTC_SCHED_L1: return VAR_L1;
+        case GTC_SCHED_HOT32K: return VAR_HOT;
+        case GTC_SCHED_HOT24K: return VAR_HOT24;
+        case GTC_SCHED_HOT16K: return VAR_HOT16;
+        case GTC_SCHED_HOT8K: return VAR_HOT8;
+        default: break;
+    }
     int& v = u.variant[MODE][weighted ? 1 : 0];
     if (v >= 0) return v;
-    if (const char* e = std::getenv("GTC_SWEEP_VARIANT")) {  // pinned for experiments
-        // 0 L1, 1 HOT, 3 HOT24, 4 HOT16, 5 HOT8 (2 is the segmented sweep,
-        // chosen elsewhere)
-        const int k = std::atoi(e);
-        v = k == 1 ? VAR_HOT : k == 3 ? VAR_HOT24 : k == 4 ? VAR_HOT16 : k == 5 ? VAR_HOT8
-          : VAR_L1;
-        return v;
-    }
-    cudaEvent_t e0, e1;
-    GTC_CUDA(cudaEventCreate(&e0));
-    GTC_CUDA(cudaEventCreate(&e1));
+    Timer trial(s);
     float best = 0.f;
     int best_v = VAR_L1;
     for (int rep = 0; rep < 2; ++rep) {  // the first round warms caches up
         for (int c = 0; c < N_VARIANTS; ++c) {
-            GTC_CUDA(cudaEventRecord(e0, s));
+            trial.start();
             launch_sweep<MODE>(c, A, weighted, s);
-            GTC_CUDA(cudaEventRecord(e1, s));
-            GTC_CUDA(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            GTC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            trial.stop();
+            const float ms = (float)trial.ms();
             *L += 1;
             if (rep == 1 && (c == 0 || ms < best)) best = ms, best_v = c;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     v = best_v;
     return v;
 }
@@ -810,55 +805,14 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         A.ticket = fs.ticket.get();
         A.out = dq;
         A.x = yc, A.prev = rc, A.next = rn, A.ynext = yn;
-        const int var = tuned_variant<MODE_PAGERANK>(*U, A, W, s, &L);
-        // the segmented sweep (gtc_seg.cu) is opt-in (GTC_SWEEP_VARIANT=2): on
-        // the R-MAT graphs measured so far it is slower than the pull sweep
-        SegPlan* SP = nullptr;
-        const char* pin = std::getenv("GTC_SWEEP_VARIANT");
-        if (pin && std::atoi(pin) == 2 && seg_supported(view)) {
-            SegPlan& sp = g->seg[view.reversed ? 1 : 0];
-            if (!sp.built) build_seg(g, view, s, sp);
-            SP = &sp;
-        }
-        DevBuf<float> wseg;
-        DevBuf<double> spart;
-        DevBuf<unsigned> sticket;
-        SegArgs SA{};
-        const bool use_seg = SP != nullptr;
-        if (use_seg) {
-            if (W) {
-                wseg.alloc(SP->m, s);
-                seg_gather_weights(*SP, in.weight, wseg.get(), s);
-                L++;
-            }
-            spart.alloc(seg_part_slots(*SP), s);
-            sticket.alloc(1, s);
-            GTC_CUDA(cudaMemsetAsync(sticket.get(), 0, sizeof(unsigned), s));
-            SA.ws = wseg.get();
-            SA.pers = pers32.get();
-            SA.uniform = (float)P.uniform;
-            SA.one_minus_d = (float)(1.0 - d);
-            SA.d = (float)d;
-            SA.psink = dq + 1;
-            SA.invdeg = invdeg.get();
-            SA.sink = P.sink.get();
-            SA.part = spart.get();
-            SA.ticket = sticket.get();
-            SA.out = dq;
-        }
+        const int var = tuned_variant<MODE_PAGERANK>(*U, A, W, in.schedule, s, &L);
         // a tuning trial wrote the dangling mass of its output: restore it
         GTC_CUDA(cudaMemcpyAsync(dq + 1, dp + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
         total.start();
         while (delta >= eps) {
             A.x = yc, A.prev = rc, A.next = rn, A.ynext = yn;
             if (in.timing) sw.start();
-            if (use_seg) {
-                SA.y = yc, SA.prev = rc, SA.next = rn, SA.ynext = yn;
-                seg_sweep(*SP, SA, W, s);
-                L++;
-            } else {
-                launch_sweep<MODE_PAGERANK>(var, A, W, s);
-            }
+            launch_sweep<MODE_PAGERANK>(var, A, W, s);
             if (in.timing) sw.stop();
             L++;
             SL++;
@@ -964,7 +918,7 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         A.ticket = f1.ticket.get();
         A.out = o1;
         A.x = xc, A.prev = xc, A.next = xn;
-        const int var = tuned_variant<MODE_EIGEN>(*U, A, W, s, &L);
+        const int var = tuned_variant<MODE_EIGEN>(*U, A, W, in.schedule, s, &L);
         total.start();
         while (delta >= eps) {
             A.x = xc, A.prev = xc, A.next = xn;
@@ -1202,7 +1156,7 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     A.ynext = atl.get();
     float *lc = lam0.get(), *ln = lam1.get();
     A.x = lc, A.prev = lc, A.next = ln;
-    const int var = tuned_variant<MODE_ADJOINT>(*U, A, W, s, &L);
+    const int var = tuned_variant<MODE_ADJOINT>(*U, A, W, GTC_SCHED_AUTO, s, &L);
 
     const uint64_t max_iter = in.params.max_iter;
     const double tol = in.params.epsilon * gnorm;

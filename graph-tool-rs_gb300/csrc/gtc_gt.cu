@@ -452,7 +452,7 @@ int gtc_gt_graph(const gtc_gt_file* f, gtc_graph** out) {
             GTC_CUDA(cudaMemcpyAsync(d_eoff.get(), f->e_off.data(), (n + 1) * sizeof(uint32_t),
                                      cudaMemcpyHostToDevice, s));
             GTC_CUDA(cudaMemsetAsync(d_bad.get(), 0xFF, sizeof(unsigned), s));
-            const unsigned blocks = grid_for(n * 32, 256, (unsigned)kSMs * 8);
+            const unsigned blocks = grid_for(n * 32, 256, (unsigned)sm_count() * 8);
             k_gt_decode<<<blocks, 256, 0, s>>>(n, d_adj.get(), d_at.get(), d_eoff.get(), f->width,
                                                f->big ? 1 : 0, d_src.get(), d_tgt.get(),
                                                d_bad.get());

@@ -138,45 +138,6 @@ struct PprSched {
     bool built = false;
 };
 
-// Segmented pull plan of one unfiltered view (gtc_seg.cu): entries sorted by
-// (source segment, destination group, destination), pair sums per
-// (segment, destination), kept with the graph.
-struct SegPlan {
-    uint32_t n = 0, m = 0, nseg = 0, ngroups = 0, npairs = 0, nunits = 0, nitems = 0;
-    DevBuf<uint16_t> src16;           // per entry: local source | pair start << 15
-    DevBuf<uint32_t> seid;            // per entry: edge id (weights are gathered through it)
-    DevBuf<uint32_t> unit_e, unit_o;  // per unit: first entry (+1 end), output of its first pair
-    DevBuf<uint4> items;              // phase-1 CTA items {segment, first unit, end unit, 0}
-    DevBuf<uint16_t> pdest;           // per pair (group order): local destination | run start << 15
-    DevBuf<uint32_t> gpair;           // per destination group: first pair (ngroups + 1)
-    DevBuf<float> partial;            // per pair: the sweep's pair sums (scratch)
-    bool built = false;
-};
-
-// Arguments of one segmented PageRank sweep.
-struct SegArgs {
-    uint32_t n, ngroups, nitems;
-    const uint16_t* src16;
-    const float* ws;        // weights in entry order, or null
-    const float* y;         // rank / deg of the current iterate
-    const uint32_t *unit_e, *unit_o;
-    const uint4* items;
-    float* partial;
-    const uint16_t* pdest;
-    const uint32_t* gpair;
-    const float* pers;      // null: uniform
-    float uniform, one_minus_d, d;
-    const double* psink;    // dangling mass of the current iterate
-    const float* prev;
-    float* next;
-    float* ynext;
-    const float* invdeg;
-    const uint8_t* sink;
-    double* part;           // per phase-2 CTA: (change, dangling mass)
-    unsigned* ticket;
-    double* out;            // [0] L1 change, [1] dangling mass of next
-};
-
 }  // namespace gtc
 
 namespace gtc {
@@ -262,7 +223,6 @@ struct gtc_graph {
     gtc::Units units_in, units_out;  // pull schedules of the plain and reversed views
     gtc::PprSched ppr_sched[2];      // batched schedules of the plain and reversed views
     gtc::DevBuf<float> ppr_z[2];     // batched iterates, kept between calls (grown on demand)
-    gtc::SegPlan seg[2];             // segmented pull plans of the plain and reversed views
     uint64_t launches = 0;  // kernels this handle has launched (diagnostics)
 };
 
@@ -291,6 +251,7 @@ struct SolveIn {
     int x_dtype = GTC_F64;
     uint64_t had = 0;            // slots the caller's map already had
     int precision = GTC_PREC_F32;
+    int schedule = GTC_SCHED_AUTO;  // gtc_schedule: the FP32 sweep kernel, or the autotuner
     bool timing = false;
 };
 
@@ -310,14 +271,6 @@ void batch_layout(gtc_graph_batch* b, uint32_t* d_src, uint32_t* d_tgt, cudaStre
 void pagerank_batch(gtc_graph_batch* b, const DVec& weight, double damping, double epsilon,
                     uint64_t max_iter, void* out, int out_dtype, uint64_t* iters, bool timing,
                     gtc_result* res, cudaStream_t s);
-
-// segmented pull sweep (gtc_seg.cu)
-struct View;
-bool seg_supported(const View& view);
-void build_seg(gtc_graph* g, const View& view, cudaStream_t s, SegPlan& P);
-void seg_gather_weights(const SegPlan& P, const DVec& w, float* ws, cudaStream_t s);
-void seg_sweep(const SegPlan& P, SegArgs A, bool weighted, cudaStream_t s);
-uint32_t seg_part_slots(const SegPlan& P);
 
 // Inputs of the PageRank adjoint (device vectors, original labels).
 struct AdjointIn {
@@ -345,6 +298,7 @@ struct PprIn {
     void* out = nullptr;              // device [B][n] ranks (original labels)
     int out_dtype = GTC_F64;
     uint64_t* iters = nullptr;        // host, B: sweeps of every column
+    int gather = GTC_PPR_BULK;        // gtc_ppr_gather
     bool timing = false;
 };
 void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* res,
@@ -448,7 +402,9 @@ __device__ __forceinline__ double warp_sum_f64(double v) {
     return v;
 }
 
-constexpr int kSMs = 152;
+// Streaming multiprocessors of the current device (queried once per device);
+// persistent grids are sized from it.
+int sm_count();
 
 inline unsigned grid_for(size_t work, unsigned per_block, unsigned cap = 1u << 20) {
     size_t b = (work + per_block - 1) / per_block;

@@ -24,7 +24,10 @@ namespace {
 
 constexpr uint32_t NA_MAX_N = 1u << 20;  // the vertex limit of the entry point
 constexpr int NA_NT = 256;
-constexpr int NA_BLOCKS = kSMs * 4;      // fixed grid of the sweep
+// Fixed grid of the sweep (4 CTAs per SM of a 152-SM part); the grid sizes
+// the per-CTA partials of the scratch array, and any size gives the same
+// result up to the FP64 fold order of those partials.
+constexpr int NA_BLOCKS = 608;
 
 // Layout of the scratch array (offsets in bytes, each 256-aligned).
 constexpr size_t NA_VEC = ((size_t)(NA_MAX_N + 1) * sizeof(float) + 255) & ~(size_t)255;
@@ -156,10 +159,13 @@ extern "C" int gtc_pagerank_noalloc(uint64_t n, const uint32_t* d_off, const uin
         GTC_REQUIRE(n <= NA_MAX_N, GTC_ERR_ARG,
                     "gtc_pagerank_noalloc: more vertices than its static scratch holds (limit "
                     "1048576)");
-        GTC_REQUIRE(n == 0 || (d_off && d_src && d_out_degree && d_rank), GTC_ERR_ARG,
-                    "gtc_pagerank_noalloc: a device array is NULL");
         GTC_REQUIRE(!(damping != damping) && !(epsilon != epsilon), GTC_ERR_ARG,
                     "gtc_pagerank_noalloc: damping or epsilon is NaN");
+        GTC_REQUIRE(max_iter != 0 || epsilon > 0.0, GTC_ERR_ARG,
+                    "gtc_pagerank_noalloc: max_iter = 0 (uncapped) with epsilon <= 0 would never "
+                    "stop");
+        GTC_REQUIRE(n == 0 || (d_off && d_src && d_out_degree && d_rank), GTC_ERR_ARG,
+                    "gtc_pagerank_noalloc: a device array is NULL");
         cudaStream_t s = (cudaStream_t)stream;
         unsigned char* base = scratch_for_current_device();
         if (iters_out) *iters_out = 0;

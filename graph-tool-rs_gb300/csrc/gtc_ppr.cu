@@ -562,9 +562,15 @@ __global__ void __launch_bounds__(PB_NT) k_ppr_bulk(PprArgs A) {
         hB ^= 1u;
     }
     if (!ok) {
-        // give the copies still in flight a bounded chance to land and report;
-        // the host discards this sweep
+        // Report, then give every copy still in flight a bounded chance to
+        // land before the block exits (its shared memory may go to another
+        // block next): the copies into the half whose wait gave up (batch C,
+        // half hB ^ 1) and the ones just issued into half hB (batch B).  The
+        // host reads the flag and fails the call (GTC_ERR_CUDA) instead of
+        // using this sweep.
         if (lane == 0) atomicExch(A.err, 1);
+        const uint32_t hf = hB ^ 1u;
+        if (bC.valid && bC.cnt > 0) (void)mbar_wait(bar0 + 8 * hf, (parity >> hf) & 1u);
         if (bB.valid && bB.cnt > 0) (void)mbar_wait(bar0 + 8 * hB, (parity >> hB) & 1u);
     }
     // the CTA's per-slot sums (warps in order, FP64) into its partial record
@@ -944,20 +950,6 @@ inline uint32_t ppr_lines(uint32_t active) {
     return c <= 4 ? c : (c <= 6 ? 6 : (c + 3) / 4 * 4);
 }
 
-// GTC_PPR_HANDOFF=k overrides the column count at which the batch hands its
-// last columns to the single-vector solver (for measurements).
-uint32_t ppr_handoff() {
-    const char* e = std::getenv("GTC_PPR_HANDOFF");
-    return e ? (uint32_t)std::atoi(e) : PPR_HANDOFF;
-}
-
-// GTC_PPR_VARIANT=regs|bulk pins the gather variant (default bulk).
-int ppr_variant() {
-    const char* e = std::getenv("GTC_PPR_VARIANT");
-    if (e && std::strcmp(e, "regs") == 0) return PPR_REGS;
-    return PPR_BULK;
-}
-
 }  // namespace
 
 void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* res,
@@ -1098,7 +1090,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     DevBuf<uint2> dpairs(s_in, s);
     DevBuf<int> derr(1, s);
     GTC_CUDA(cudaMemsetAsync(derr.get(), 0, sizeof(int), s));
-    const int variant = ppr_variant();
+    const int variant = in.gather == GTC_PPR_REGS ? PPR_REGS : PPR_BULK;
 
     PprArgs A{};
     A.n = n;
@@ -1124,7 +1116,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     float *zc = z0.get(), *zx = z1.get();
     PprTimer total(s), tsw(s);
     total.start();
-    const uint32_t handoff = ppr_handoff();
+    const uint32_t handoff = PPR_HANDOFF;
     while (running > 0) {
         // the output layout: the columns still running, packed
         out_slot.assign(s_in, PPR_NONE);

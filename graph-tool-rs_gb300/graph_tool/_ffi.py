@@ -43,7 +43,22 @@ class View(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("schedule", C.c_int32), ("stream", C.c_void_p),
-                ("timing", C.c_int32), ("reserved", C.c_int32)]
+                ("timing", C.c_int32), ("ppr_gather", C.c_int32)]
+
+
+# gtc_schedule: the FP32 sweep kernels (every one computes the same values)
+GTC_SCHED_AUTO = 0
+GTC_SCHED_L1 = 1
+GTC_SCHED_HOT32K = 2
+GTC_SCHED_HOT24K = 3
+GTC_SCHED_HOT16K = 4
+GTC_SCHED_HOT8K = 5
+SCHEDULES = {"auto": GTC_SCHED_AUTO, "l1": GTC_SCHED_L1, "hot32k": GTC_SCHED_HOT32K,
+             "hot24k": GTC_SCHED_HOT24K, "hot16k": GTC_SCHED_HOT16K, "hot8k": GTC_SCHED_HOT8K}
+
+# gtc_ppr_gather: the batched PPR gather kernels
+GTC_PPR_BULK = 0
+GTC_PPR_REGS = 1
 
 
 class Result(C.Structure):

@@ -248,22 +248,24 @@ class Graph:
                  epsilon: float = 1e-6, max_iter: int = 0, grain: int = 4096,
                  reversed: bool = False, vfilt=None, efilt=None,
                  precision: str = "f32", stream=None, result: bool = False,
-                 plan_len: int | None = None):
+                 plan_len: int | None = None, schedule: str = "auto"):
         """pagerank / pagerank_with (crates/gt-algo/src/centrality.rs:234-384)
         on this graph, its reversal or a filtered view.  ``rank`` is the
         initial iterate and the output; returns the number of sweeps (and the
-        full gtc_result when ``result``)."""
+        full gtc_result when ``result``).  ``schedule`` pins one FP32 sweep
+        kernel (``_ffi.SCHEDULES``; "auto" lets the autotuner choose)."""
         return _solve(self, "pagerank", rank, weight, pers, damping, epsilon, max_iter, grain,
-                      reversed, vfilt, efilt, precision, stream, result, plan_len)
+                      reversed, vfilt, efilt, precision, stream, result, plan_len, schedule)
 
     def eigenvector(self, x: PropertyMap, weight: PropertyMap | None = None,
                     epsilon: float = 1e-6, max_iter: int = 0, grain: int = 4096,
                     reversed: bool = False, vfilt=None, efilt=None, precision: str = "f32",
-                    stream=None, result: bool = False, plan_len: int | None = None):
+                    stream=None, result: bool = False, plan_len: int | None = None,
+                    schedule: str = "auto"):
         """eigenvector (crates/gt-algo/src/centrality.rs:405-497); returns
         (eigenvalue, sweeps)."""
         r = _solve(self, "eigenvector", x, weight, None, 0.0, epsilon, max_iter, grain, reversed,
-                   vfilt, efilt, precision, stream, True, plan_len)
+                   vfilt, efilt, precision, stream, True, plan_len, schedule)
         return r if result else (r.eigenvalue, r.iterations)
 
     def weighted_degree(self, weight: PropertyMap | None = None, direction: str = "out",
@@ -314,14 +316,18 @@ class Graph:
 
     def ppr_batch(self, seeds, values=None, weight: PropertyMap | None = None,
                   damping: float = 0.85, epsilon: float = 1e-6, max_iter: int = 0,
-                  reversed: bool = False):
+                  reversed: bool = False, gather: str = "bulk"):
         """Personalised PageRank for many seed sets at once.
 
         ``seeds`` is a list of B vertex-index sequences (1 <= B <= 512);
         ``values`` (optional) the matching personalisation values (default
         1/|set|).  Every vector is pagerank_with (centrality.rs:261-384) with
         that sparse personalisation, started from it, to ``epsilon``.
+        ``gather`` picks the batched sweep's gather kernel ("bulk": rows staged
+        by cp.async.bulk, the default; "regs": rows loaded into registers).
         Returns (ranks float64 [B][n], sweeps uint64 [B])."""
+        if gather not in ("bulk", "regs"):
+            raise ValueError("gather must be 'bulk' or 'regs'")
         B = len(seeds)
         n = self.num_vertices()
         off = np.zeros(B + 1, np.uint64)
@@ -339,11 +345,13 @@ class Graph:
         view = _ffi.View(int(bool(reversed)), 0, None, 0, None, 0)
         params = _ffi.PowerIteration(float(epsilon), int(max_iter or 0), n, max(-(-n // 4096), 1))
         res = _ffi.Result()
+        opt = _ffi.Options(_ffi.GTC_PREC_F32, 0, None, 0,
+                           _ffi.GTC_PPR_REGS if gather == "regs" else _ffi.GTC_PPR_BULK)
         _ffi.check(_ffi.lib().gtc_ppr_batch(
             self.handle(), C.byref(view), _ffi.ptr(w, _ffi.f64p), 0 if w is None else w.size, B,
             _ffi.ptr(off, _ffi.u64p), _ffi.ptr(verts, _ffi.u32p), _ffi.ptr(vals, _ffi.f64p),
             float(damping), C.byref(params), _ffi.ptr(ranks, _ffi.f64p), _ffi.ptr(iters, _ffi.u64p),
-            None, C.byref(res)))
+            C.byref(opt), C.byref(res)))
         return ranks, iters
 
 
@@ -443,7 +451,7 @@ def _mask(g: Graph, m, bound: int):
 
 
 def _solve(g: Graph, kind, out_map, weight, pers, damping, epsilon, max_iter, grain, reversed,
-           vfilt, efilt, precision, stream, want_result, plan_len=None):
+           vfilt, efilt, precision, stream, want_result, plan_len=None, schedule="auto"):
     if not isinstance(out_map, PropertyMap):
         raise ValueError("the output must be a vertex PropertyMap of 'double'")
     if out_map._g is not g or out_map.key_type() != "v" or out_map.value_type() != "double":
@@ -452,6 +460,8 @@ def _solve(g: Graph, kind, out_map, weight, pers, damping, epsilon, max_iter, gr
         raise ValueError("Plan::new: grain must be non-zero")
     if precision not in _PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
+    if schedule not in _ffi.SCHEDULES:
+        raise ValueError(f"schedule must be one of {sorted(_ffi.SCHEDULES)}")
     n = g.num_vertices()
     w = _f64_map(g, weight, "e", "weight")
     p = _f64_map(g, pers, "v", "pers")
@@ -464,7 +474,7 @@ def _solve(g: Graph, kind, out_map, weight, pers, damping, epsilon, max_iter, gr
     # PowerIteration.plan: Plan::new(plan_len, grain); plan_len must be n
     pl = n if plan_len is None else int(plan_len)
     params = _ffi.PowerIteration(float(epsilon), int(max_iter or 0), pl, max(-(-pl // grain), 1))
-    opt = _ffi.Options(_PRECISIONS[precision], 0, stream, 0, 0)
+    opt = _ffi.Options(_PRECISIONS[precision], _ffi.SCHEDULES[schedule], stream, 0, 0)
     res = _ffi.Result()
     L = _ffi.lib()
     h = g.handle()

@@ -101,13 +101,34 @@ typedef struct gtc_view {
     uint64_t emask_len;
 } gtc_view;
 
+/* Sweep kernels of the GTC_PREC_F32 PageRank and eigenvector solves.  Every
+ * kernel computes the same values (the per-row sums and the reductions do
+ * not depend on the schedule), so a choice changes speed only.  AUTO times
+ * the candidates on the first solve of a (graph view, mode, weighting) and
+ * caches the fastest on the handle. */
+typedef enum gtc_schedule {
+    GTC_SCHED_AUTO = 0,
+    GTC_SCHED_L1 = 1,      /* in-degree tiers, every gather through L1/L2        */
+    GTC_SCHED_HOT32K = 2,  /* in-degree tiers, the 32,768 most gathered entries
+                              of the gathered vector in shared memory            */
+    GTC_SCHED_HOT24K = 3,  /* ... 24,576 entries                                 */
+    GTC_SCHED_HOT16K = 4,  /* ... 16,384 entries                                 */
+    GTC_SCHED_HOT8K = 5    /* ... 8,192 entries                                  */
+} gtc_schedule;
+
+/* Gather kernels of the batched personalised PageRank (gtc_ppr_batch). */
+typedef enum gtc_ppr_gather {
+    GTC_PPR_BULK = 0,  /* rows of the iterate staged by cp.async.bulk (default) */
+    GTC_PPR_REGS = 1   /* rows gathered into registers                         */
+} gtc_ppr_gather;
+
 /* Per-call options.  A NULL pointer means all defaults. */
 typedef struct gtc_options {
-    int32_t precision;  /* gtc_precision, default GTC_PREC_F32             */
-    int32_t schedule;   /* 0 = autotuned; otherwise a fixed unit size       */
-    void* stream;       /* cudaStream_t to run on; NULL = the handle's     */
-    int32_t timing;     /* non-zero: time every sweep kernel (sweep_ms)    */
-    int32_t reserved;
+    int32_t precision;   /* gtc_precision, default GTC_PREC_F32                */
+    int32_t schedule;    /* gtc_schedule, default GTC_SCHED_AUTO               */
+    void* stream;        /* cudaStream_t to run on; NULL = the handle's        */
+    int32_t timing;      /* non-zero: time every sweep kernel (sweep_ms)       */
+    int32_t ppr_gather;  /* gtc_ppr_gather, default GTC_PPR_BULK               */
 } gtc_options;
 
 /* What a solve reports back. */
@@ -411,13 +432,16 @@ int gtc_pagerank_adjoint_device(gtc_graph* g, const gtc_view* view, const gtc_dv
  *                 (pagerank with a Unity weight, centrality.rs:234-248)
  *   stream        a cudaStream_t (NULL = the legacy default stream)
  *
- * FP32 vectors, compensated row sums, FP64 delta and dangling mass.  All
- * calls share the static array and it keeps the last call's contents (each
- * call clears what must start at zero); calls that overlap on the GPU race.
+ * FP32 vectors, compensated row sums, FP64 delta and dangling mass.  There
+ * is one static array per GPU and every call on that GPU shares it; it keeps
+ * the last call's contents (each call clears what must start at zero), and
+ * calls that overlap on the GPU (two streams, two host threads) race on it.
+ * max_iter = 0 with epsilon <= 0 would never stop and is GTC_ERR_ARG.
  * The first call on a device does a one-time set-up: it looks the array's
  * device address up (cudaGetSymbolAddress with that device current).  Make
- * that first call before any stream capture.  Returns when the result is in
- * d_rank. */
+ * that first call before any stream capture.  The call is blocking: after
+ * every sweep it waits for the stream to read the L1 change on the host,
+ * and it returns when the result is in d_rank. */
 int gtc_pagerank_noalloc(uint64_t n, const uint32_t* d_off, const uint32_t* d_src,
                          const uint32_t* d_out_degree, double damping, double epsilon,
                          uint64_t max_iter, float* d_rank, uint64_t* iters_out, void* stream);

@@ -16,7 +16,8 @@ def _seed_sets(n, B, rng, max_size=8):
     return sets
 
 
-def _check(oracle, gtc, n, src, tgt, B, weight=None, reversed=False, eps=1e-7, seed=1):
+def _check(oracle, gtc, n, src, tgt, B, weight=None, reversed=False, eps=1e-7, seed=1,
+           gather="bulk"):
     rng = np.random.default_rng(seed)
     sets = _seed_sets(n, B, rng)
     g = gtc.Graph()
@@ -26,7 +27,8 @@ def _check(oracle, gtc, n, src, tgt, B, weight=None, reversed=False, eps=1e-7, s
     if weight is not None:
         wm = g.new_edge_property("double")
         wm.a[:] = weight
-    ranks, iters = g.ppr_batch(sets, weight=wm, epsilon=eps, max_iter=1000, reversed=reversed)
+    ranks, iters = g.ppr_batch(sets, weight=wm, epsilon=eps, max_iter=1000, reversed=reversed,
+                               gather=gather)
     og = oracle.Graph(n)
     og.add_edge_arrays(src, tgt)
     worst = 0.0
@@ -43,24 +45,23 @@ def _check(oracle, gtc, n, src, tgt, B, weight=None, reversed=False, eps=1e-7, s
 
 
 @pytest.fixture(params=["bulk", "regs"])
-def variant(request, monkeypatch):
+def variant(request):
     """Both gather variants of the batched sweep (bulk copies into shared
     memory, loads into registers) must give the oracle's results."""
-    monkeypatch.setenv("GTC_PPR_VARIANT", request.param)
     return request.param
 
 
 def test_ppr_batch_matches_separate_solves(oracle, gtc, variant):
     from graph_tool import synth
     n, src, tgt, _ = synth.erdos_renyi_sinks(n=3000, m=24000)
-    _check(oracle, gtc, n, src, tgt, 37)
+    _check(oracle, gtc, n, src, tgt, 37, gather=variant)
 
 
 def test_ppr_batch_padded_columns_weighted(oracle, gtc, variant):
     from graph_tool import synth
     n, src, tgt = synth.rmat_cpu(11, edge_factor=8, seed=4)
     w = np.random.default_rng(2).uniform(0.1, 1.0, src.size)
-    _check(oracle, gtc, n, src, tgt, 130, weight=w, seed=3)
+    _check(oracle, gtc, n, src, tgt, 130, weight=w, seed=3, gather=variant)
 
 
 def test_ppr_batch_reversed_with_hubs(oracle, gtc, variant):
@@ -70,8 +71,10 @@ def test_ppr_batch_reversed_with_hubs(oracle, gtc, variant):
     src = rng.integers(0, n, m)
     tgt = rng.integers(0, n, m)
     tgt[: 6000] = 7
-    _check(oracle, gtc, n, src.astype(np.uint32), tgt.astype(np.uint32), 64, seed=6)
-    _check(oracle, gtc, n, src.astype(np.uint32), tgt.astype(np.uint32), 64, seed=7, reversed=True)
+    _check(oracle, gtc, n, src.astype(np.uint32), tgt.astype(np.uint32), 64, seed=6,
+           gather=variant)
+    _check(oracle, gtc, n, src.astype(np.uint32), tgt.astype(np.uint32), 64, seed=7, reversed=True,
+           gather=variant)
 
 
 def test_ppr_batch_max_iter_caps_every_column(oracle, gtc, variant):
@@ -84,7 +87,7 @@ def test_ppr_batch_max_iter_caps_every_column(oracle, gtc, variant):
     g = gtc.Graph()
     g.add_vertex(n)
     g.add_edges(src, tgt)
-    ranks, iters = g.ppr_batch(sets, epsilon=1e-12, max_iter=5)
+    ranks, iters = g.ppr_batch(sets, epsilon=1e-12, max_iter=5, gather=variant)
     assert (iters == 5).all()
     og = oracle.Graph(n)
     og.add_edge_arrays(src, tgt)
