@@ -42,10 +42,17 @@ More measurements ride on the same line (skipped with --no-secondary):
   betweenness  Brandes from every vertex of an R-MAT scale-14 graph (edge
             factor 16, deduplicated): GPU time against the CPU oracle on all
             host threads, edges x sources per second, and their difference.
-  eigenvector  eigenvector centrality on the weighted Chung-Lu graph,
-            epsilon 1e-7, max_iter 500: time, sweeps, eigenvalue, roofline.
+  chunglu   the weighted Chung-Lu graph (n=4,194,304, m~67M): weighted
+            PageRank (epsilon 1e-7) and eigenvector centrality (epsilon 1e-7,
+            max_iter 500), each with time, sweeps, roofline and its error
+            against the oracle's f64 solve.
+  weighted  the headline graph with FP32 weights U(0.1,1): GTEPS, roofline
+            (W = 1), error against the oracle's f64 solve.
+  exact_f64 the headline graph in GTC_PREC_F64_EXACT (the reference's
+            arithmetic): GTEPS and bit identity with the oracle.
+  build     time to build the headline graph's handle on the GPU.
 
-``--section adjoint|ppr_batch|graph_batch|betweenness|eigenvector`` runs one of them alone and prints
+``--section adjoint|ppr_batch|graph_batch|betweenness|chunglu`` runs one of them alone and prints
 its JSON (``--ppr-scale``, ``--ppr-b``, ``--graphs`` shrink the last two for
 profiling; ``--workload`` picks the adjoint's graph).
 
@@ -279,6 +286,10 @@ def ppr_section(L, device, stream, B=256, sequential=True, scale=22):
     n, src, tgt = synth_gpu.rmat(scale, 16, seed=3, device=device)
     m = int(src.numel())
     torch.cuda.synchronize()
+    src_np = tgt_np = None
+    if sequential:  # the full measurement also checks columns against the oracle
+        src_np = src.cpu().numpy().astype(np.uint32)
+        tgt_np = tgt.cpu().numpy().astype(np.uint32)
     h = C.c_void_p()
     _ffi.check(L.gtc_graph_create_device(n, m, C.c_void_p(src.data_ptr()),
                                          C.c_void_p(tgt.data_ptr()),
@@ -339,7 +350,8 @@ def ppr_section(L, device, stream, B=256, sequential=True, scale=22):
     seq()  # warm-up
     seq_sweeps.clear()
     t_s, _ = _events_ms(seq, stream, 1)
-    # agreement of the two on a sample of columns
+    # agreement of the two on a sample of columns, and of the batch with the
+    # oracle's pagerank_with of the same seed sets
     errs = []
     for b in range(0, B, 37):
         r = _ffi.Result()
@@ -348,6 +360,22 @@ def ppr_section(L, device, stream, B=256, sequential=True, scale=22):
         a = ranks[b * n:(b + 1) * n].double()
         errs.append(float((a - one.double()).abs().sum() / one.double().abs().sum()))
     _ffi.check(L.gtc_graph_destroy(h))
+    oracle_cols = []
+    if src_np is not None:
+        import oracle as O
+        threads = os.cpu_count() or 1
+        og = O.Graph(n)
+        og.add_edge_arrays(src_np, tgt_np)
+        for b in range(0, B, 37):
+            pv = np.zeros(n)
+            pv[sets[b]] = 1.0 / len(sets[b])
+            want, it_o = og.pagerank(pers=pv, damping=DAMPING, epsilon=eps, max_iter=MAX_ITER,
+                                     grain=4096, threads=threads)
+            got = ranks[b * n:(b + 1) * n].double().cpu().numpy()
+            p = _parity(got, want, batch_sweeps[b], it_o, "gtc_oracle.c pagerank_with")
+            p["column"] = b
+            oracle_cols.append(p)
+        del og
     return {"workload": f"rmat{scale} (n={n}, m={m}), B={B} seed sets of 1-64 vertices, eps {eps}",
             "batched_solves_per_s": B / (t_b / 1e3), "sequential_solves_per_s": B / (t_s / 1e3),
             "speedup_vs_sequential": t_s / t_b, "batched_ms": t_b, "sequential_ms": t_s,
@@ -357,7 +385,11 @@ def ppr_section(L, device, stream, B=256, sequential=True, scale=22):
                                           int(np.percentile(batch_sweeps, 90)),
                                           int(batch_sweeps.max())],
             "sequential_sweeps_mean": float(np.mean(seq_sweeps)),
-            "max_rel_l1_batched_vs_single": max(errs)}
+            "max_rel_l1_batched_vs_single": max(errs),
+            "parity_vs_f64_oracle": {
+                "columns": oracle_cols,
+                "max_rel_l1": max((c["rel_l1"] for c in oracle_cols), default=None),
+                "max_abs": max((c["max_abs"] for c in oracle_cols), default=None)}}
 
 
 def sbm_batch_gpu(G, device, seed=33, n_min=100, n_max=100_000, blocks=4, k_in=16.0, k_out=2.0):
@@ -412,6 +444,12 @@ def graph_batch_section(L, device, stream, G=4096):
     t0 = time.perf_counter()
     b = GraphBatch(graphs)
     build_s = time.perf_counter() - t0
+    # graphs checked against the oracle's solve of that graph alone: the
+    # smallest, the largest, and a spread in between
+    order = np.argsort(sizes, kind="stable")
+    picks = sorted({int(order[0]), int(order[-1])} |
+                   {int(order[i]) for i in np.linspace(0, G - 1, 8).astype(int)})
+    sample = {k: graphs[k] for k in picks}
     del graphs, src, tgt
     n, m = int(b.voff[-1]), int(b.eoff[-1])
     gen = torch.Generator(device=device)
@@ -435,22 +473,139 @@ def graph_batch_section(L, device, stream, G=4096):
     solve()  # captures the solve into a CUDA graph
     t_ms, _ = _events_ms(solve, stream, 3)
     edge_sweeps = float((iters.astype(np.float64) * counts).sum())
+    import oracle as O
+    voff = np.asarray(b.voff, np.int64)
+    w_all = w.double().cpu().numpy()
+    r_all = ranks.double().cpu().numpy()
+    checked = []
+    for k, (nk, sk, tk) in sample.items():
+        og = O.Graph(nk)
+        og.add_edge_arrays(sk, tk)
+        want, it_o = og.pagerank(weight=w_all[eoff[k]:eoff[k + 1]], damping=DAMPING, epsilon=1e-6,
+                                 max_iter=1000, grain=4096, threads=1)
+        p = _parity(r_all[voff[k]:voff[k + 1]], want, iters[k], it_o,
+                    "gtc_oracle.c f64 pagerank of this graph alone")
+        p["graph"], p["n"], p["m"] = k, nk, int(sk.size)
+        checked.append(p)
     return {"workload": f"{G} SBM graphs (n 100-100000 log-uniform, 4 blocks, p_in 16/n, "
                         f"p_out 2/n), FP32 weights U(0.1,1), eps 1e-6",
             "graphs": G, "n": n, "m": m, "solve_ms": t_ms, "graphs_per_s": G / (t_ms / 1e3),
             "gteps": edge_sweeps / (t_ms / 1e3) / 1e9,
             "sweeps_mean": float(iters.mean()), "sweeps_max": int(iters.max()),
             "build_s": build_s, "kernel_launches_per_solve": launches[0],
-            "cuda_graph_launches_per_solve": 1}
+            "cuda_graph_launches_per_solve": 1,
+            "parity_vs_f64_oracle": {
+                "graphs": checked, "max_rel_l1": max(c["rel_l1"] for c in checked),
+                "max_abs": max(c["max_abs"] for c in checked),
+                "max_sweep_difference": max(abs(c["sweeps_gpu"] - c["sweeps_oracle"])
+                                            for c in checked)}}
 
 
-def eigenvector_section(L, device, stream):
-    """Eigenvector centrality (centrality.rs:405-497 of graph-tool-rs) on the
-    Chung-Lu graph (n = 4,194,304, m ~ 67M, FP32 weights U(0.1, 1)), epsilon
-    1e-7, max_iter 500: time per solve and per sweep, the sweep count, the
-    eigenvalue, and the sweep kernel against the HBM roofline
-    (B_ev = 4(n+1) + 8m + 12n bytes a sweep)."""
+def _parity(got, want, sweeps_gpu, sweeps_oracle, what):
+    import numpy as np
+    diff = np.abs(got - want)
+    return {"rel_l1": float(diff.sum() / np.abs(want).sum()), "max_abs": float(diff.max()),
+            "sweeps_gpu": int(sweeps_gpu), "sweeps_oracle": int(sweeps_oracle),
+            "reference": what}
+
+
+def _timed_solves(solve, stream, reps):
+    """Warm-up solve, then `reps` timed ones: (ms per solve, results)."""
+    solve()
+    return _events_ms(solve, stream, reps)
+
+
+def weighted_section(L, h, n, m, device, stream, og, threads):
+    """Weighted PageRank on the headline R-MAT graph (FP32 weights U(0.1, 1),
+    the workload 'rmat24w'): the weighted branch of the sweep
+    (centrality.rs:355-365, (prev[s] * w) / ds), its roofline (W = 1) and its
+    error against the oracle's complete f64 solve of the same graph."""
     import torch
+    from graph_tool import _ffi, synth_gpu
+    wl = WORKLOADS["rmat24w"]
+    u = synth_gpu._unit(synth_gpu.splitmix(wl["seed"] + 1000, 0, m, device))
+    w = (0.1 + 0.9 * u).to(torch.float32)
+    wv = _ffi.DVec.of(w)
+    rank_t = torch.empty(n, dtype=torch.float32, device=device)
+    rv = _ffi.DVec.of(rank_t)
+    params = _ffi.PowerIteration(wl["eps"], MAX_ITER, n, (n + 4095) // 4096)
+    opt = _ffi.Options(_ffi.GTC_PREC_F32, 0, C.c_void_p(stream.cuda_stream), 1, 0)
+    runs = []
+
+    def solve():
+        r = _ffi.Result()
+        _ffi.check(L.gtc_pagerank_device(h, None, C.byref(wv), None, DAMPING, C.byref(params),
+                                         C.byref(rv), 0, C.byref(opt), C.byref(r)))
+        runs.append(r)
+        return r
+
+    solve()  # the autotuner's trials
+    runs.clear()
+    t_ms, _ = _timed_solves(solve, stream, 5)
+    runs = runs[1:]
+    sweeps = sum(int(r.iterations) for r in runs)
+    sweep_s = sum(r.sweep_ms for r in runs) / 1e3 / max(sweeps, 1)
+    peak, peak_kind = measured_peaks()
+    b = algorithmic_bytes(n, m, True)
+    out = {"workload": "rmat24w: " + wl["label"], "n": n, "m": m, "epsilon": wl["eps"],
+           "ms_per_solve": t_ms, "sweeps": int(runs[-1].iterations),
+           "gteps": m * sweeps / len(runs) / (t_ms / 1e3) / 1e9,
+           "roofline": {"bound": "hbm", "bytes_per_launch": b, "avg_launch_us": sweep_s * 1e6,
+                        "achieved": b / sweep_s / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": b / sweep_s / 1e9 / peak, "peak_kind": peak_kind}}
+    t0 = time.perf_counter()
+    want, it_o = og.pagerank(weight=w.double().cpu().numpy(), damping=DAMPING,
+                             epsilon=wl["eps"], max_iter=MAX_ITER, grain=4096, threads=threads)
+    out["parity_vs_f64_oracle"] = _parity(rank_t.double().cpu().numpy(), want,
+                                          runs[-1].iterations, it_o,
+                                          "gtc_oracle.c f64 pagerank, same graph and weights")
+    out["parity_vs_f64_oracle"]["oracle_s"] = time.perf_counter() - t0
+    return out
+
+
+def exact_section(L, h, n, m, device, stream, want):
+    """GTC_PREC_F64_EXACT on the headline graph: the reference's arithmetic
+    operation for operation (per-edge (prev[s] * w) / ds, Plan-chunk folds,
+    centrality.rs:141-167, 355-365), the precision a drop-in caller that
+    needs the reference's bits uses.  Timed, and compared bit for bit with
+    the oracle's f64 solve."""
+    import numpy as np
+    import torch
+    from graph_tool import _ffi
+    wl = WORKLOADS["rmat24"]
+    rank_t = torch.empty(n, dtype=torch.float64, device=device)
+    rv = _ffi.DVec.of(rank_t)
+    params = _ffi.PowerIteration(wl["eps"], MAX_ITER, n, (n + 4095) // 4096)
+    opt = _ffi.Options(_ffi.GTC_PREC_F64_EXACT, 0, C.c_void_p(stream.cuda_stream), 0, 0)
+    runs = []
+
+    def solve():
+        r = _ffi.Result()
+        _ffi.check(L.gtc_pagerank_device(h, None, None, None, DAMPING, C.byref(params),
+                                         C.byref(rv), 0, C.byref(opt), C.byref(r)))
+        runs.append(r)
+        return r
+
+    t_ms, _ = _timed_solves(solve, stream, 2)
+    sweeps = int(runs[-1].iterations)
+    out = {"workload": "rmat24, unweighted, GTC_PREC_F64_EXACT (Plan grain 4096)",
+           "ms_per_solve": t_ms, "sweeps": sweeps, "gteps": m * sweeps / (t_ms / 1e3) / 1e9}
+    if want is not None:
+        got = rank_t.cpu().numpy()
+        out["bit_identical_to_oracle"] = bool(got.tobytes() == np.ascontiguousarray(want).tobytes())
+        out["max_abs_vs_oracle"] = float(np.abs(got - want).max())
+    return out
+
+
+def chunglu_section(L, device, stream):
+    """The power-law Chung-Lu graph (n = 4,194,304, m ~ 67M, Pareto(2.1)
+    degrees, FP32 weights U(0.1, 1)): weighted PageRank (epsilon 1e-7,
+    uncapped) and eigenvector centrality (epsilon 1e-7, max_iter 500;
+    centrality.rs:405-497), each timed, against the HBM roofline
+    (PageRank: B_pr with W = 1; eigenvector: B_ev = 4(n+1) + 8m + 12n bytes a
+    sweep), and against the oracle's complete f64 solves of the same graph."""
+    import torch
+    import oracle as O
     from graph_tool import _ffi
     wl = WORKLOADS["chunglu"]
     n, src, tgt, w = make_graph(wl, device, 0)
@@ -459,37 +614,85 @@ def eigenvector_section(L, device, stream):
     _ffi.check(L.gtc_graph_create_device(n, m, C.c_void_p(src.data_ptr()),
                                          C.c_void_p(tgt.data_ptr()),
                                          C.c_void_p(stream.cuda_stream), C.byref(h)))
+    threads = os.cpu_count() or 1
     try:
         _ffi.check(L.gtc_graph_set_stream(h, C.c_void_p(stream.cuda_stream)))
+        src_np = src.cpu().numpy().astype("uint32")
+        tgt_np = tgt.cpu().numpy().astype("uint32")
+        w_np = w.double().cpu().numpy()
         del src, tgt
         wv = _ffi.DVec.of(w)
         x = torch.empty(n, dtype=torch.float32, device=device)
         xv = _ffi.DVec.of(x)
-        params = _ffi.PowerIteration(1e-7, 500, n, (n + 4095) // 4096)
+        peak, peak_kind = measured_peaks()
         opt = _ffi.Options(_ffi.GTC_PREC_F32, 0, C.c_void_p(stream.cuda_stream), 1, 0)
+        og = O.Graph(n)
+        og.add_edge_arrays(src_np, tgt_np)
+        out = {"workload": wl["label"], "n": n, "m": m}
+
+        # ---- weighted PageRank --------------------------------------------
+        pp = _ffi.PowerIteration(wl["eps"], 0, n, (n + 4095) // 4096)
         runs = []
 
-        def solve():
+        def pr():
             r = _ffi.Result()
-            _ffi.check(L.gtc_eigenvector_device(h, None, C.byref(wv), C.byref(params),
-                                                C.byref(xv), 0, C.byref(opt), C.byref(r)))
+            _ffi.check(L.gtc_pagerank_device(h, None, C.byref(wv), None, DAMPING, C.byref(pp),
+                                             C.byref(xv), 0, C.byref(opt), C.byref(r)))
             runs.append(r)
             return r
 
-        solve()
-        solve()  # the autotuner's trials, then a warm solve
+        pr()
         runs.clear()
-        t_ms, _ = _events_ms(solve, stream, 3)
+        t_ms, _ = _timed_solves(pr, stream, 3)
+        runs = runs[1:]
         sweeps = sum(int(r.iterations) for r in runs)
         sweep_s = sum(r.sweep_ms for r in runs) / 1e3 / max(sweeps, 1)
-        peak, peak_kind = measured_peaks()
+        b_pr = algorithmic_bytes(n, m, True)
+        want, it_o = og.pagerank(weight=w_np, damping=DAMPING, epsilon=wl["eps"], max_iter=0,
+                                 grain=4096, threads=threads)
+        out["pagerank"] = {
+            "epsilon": wl["eps"], "max_iter": 0, "ms_per_solve": t_ms,
+            "sweeps": int(runs[-1].iterations), "ms_per_sweep": sweep_s * 1e3,
+            "gteps": m * sweeps / len(runs) / (t_ms / 1e3) / 1e9,
+            "roofline": {"bound": "hbm", "bytes_per_launch": b_pr,
+                         "achieved": b_pr / sweep_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": b_pr / sweep_s / 1e9 / peak, "peak_kind": peak_kind},
+            "parity_vs_f64_oracle": _parity(x.double().cpu().numpy(), want, runs[-1].iterations,
+                                            it_o, "gtc_oracle.c f64 pagerank, same graph")}
+
+        # ---- eigenvector centrality ---------------------------------------
+        pe = _ffi.PowerIteration(1e-7, 500, n, (n + 4095) // 4096)
+        runs = []
+
+        def ev():
+            r = _ffi.Result()
+            _ffi.check(L.gtc_eigenvector_device(h, None, C.byref(wv), C.byref(pe), C.byref(xv),
+                                                0, C.byref(opt), C.byref(r)))
+            runs.append(r)
+            return r
+
+        ev()
+        runs.clear()
+        t_ms, _ = _timed_solves(ev, stream, 3)
+        runs = runs[1:]
+        sweeps = sum(int(r.iterations) for r in runs)
+        sweep_s = sum(r.sweep_ms for r in runs) / 1e3 / max(sweeps, 1)
         b_ev = 4 * (n + 1) + 8 * m + 12 * n
-        return {"workload": "Chung-Lu n=4,194,304, m~67M, FP32 weights U(0.1,1), eps 1e-7, "
-                            "max_iter 500",
-                "n": n, "m": m, "solve_ms": t_ms, "sweeps": int(runs[-1].iterations),
-                "eigenvalue": float(runs[-1].eigenvalue), "ms_per_sweep": sweep_s * 1e3,
-                "gteps": m * sweeps / 3 / (t_ms / 1e3) / 1e9,
-                "roofline_frac": b_ev / sweep_s / 1e9 / peak, "peak_kind": peak_kind}
+        want, eig_o, it_o = og.eigenvector(weight=w_np, epsilon=1e-7, max_iter=500, grain=4096,
+                                           threads=threads)
+        par = _parity(x.double().cpu().numpy(), want, runs[-1].iterations, it_o,
+                      "gtc_oracle.c f64 eigenvector, same graph")
+        par["eigenvalue_gpu"] = float(runs[-1].eigenvalue)
+        par["eigenvalue_oracle"] = float(eig_o)
+        out["eigenvector"] = {
+            "epsilon": 1e-7, "max_iter": 500, "ms_per_solve": t_ms,
+            "sweeps": int(runs[-1].iterations), "eigenvalue": float(runs[-1].eigenvalue),
+            "ms_per_sweep": sweep_s * 1e3, "gteps": m * sweeps / len(runs) / (t_ms / 1e3) / 1e9,
+            "roofline": {"bound": "hbm", "bytes_per_launch": b_ev,
+                         "achieved": b_ev / sweep_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": b_ev / sweep_s / 1e9 / peak, "peak_kind": peak_kind},
+            "parity_vs_f64_oracle": par}
+        return out
     finally:
         L.gtc_graph_destroy(h)
 
@@ -548,7 +751,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--section", choices=["adjoint", "ppr_batch", "graph_batch", "betweenness",
-                                          "eigenvector"],
+                                          "chunglu"],
                     help="run only this secondary measurement (adjoint on --workload's graph) "
                          "and print its JSON")
     ap.add_argument("--ppr-scale", type=int, default=22, help="R-MAT scale of the ppr_batch graph")
@@ -561,7 +764,7 @@ def main():
     import numpy as np
     import torch
 
-    if args.section in ("ppr_batch", "graph_batch", "betweenness", "eigenvector"):
+    if args.section in ("ppr_batch", "graph_batch", "betweenness", "chunglu"):
         from graph_tool import _ffi
         device = torch.device("cuda", local)
         torch.cuda.set_device(device)
@@ -570,8 +773,8 @@ def main():
             out = ppr_section(_ffi.lib(), device, stream, B=args.ppr_b, scale=args.ppr_scale)
         elif args.section == "betweenness":
             out = betweenness_section(_ffi.lib(), device, stream)
-        elif args.section == "eigenvector":
-            out = eigenvector_section(_ffi.lib(), device, stream)
+        elif args.section == "chunglu":
+            out = chunglu_section(_ffi.lib(), device, stream)
         else:
             out = graph_batch_section(_ffi.lib(), device, stream, G=args.graphs)
         print(json.dumps({"section": args.section, **out}), flush=True)
@@ -608,15 +811,19 @@ def main():
             tot_t += dt
             tot_it += it
         v = m * tot_it / tot_t / 1e9
-        sample = (f"{args.cpu_sweeps} sweeps of the full {args.workload} graph per step "
-                  f"(n={n}, m={m}), gtc_oracle.c pagerank with {threads} OpenMP threads")
+        sample = (f"a step is {args.cpu_sweeps} sweeps of the full {args.workload} graph "
+                  f"(n={n}, m={m}), gtc_oracle.c pagerank with {threads} OpenMP threads; "
+                  f"GTEPS = edges x sweeps / s, comparable with the GPU arm's complete solves")
         print(json.dumps({
             "impl": "reference", "metric": "PageRank GTEPS", "value": v, "unit": "GTEPS",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.workload, "graph": wl["label"], "n": n, "m": m,
-                       "damping": DAMPING, "epsilon": wl["eps"]},
+                       "damping": DAMPING, "epsilon": wl["eps"],
+                       "sweeps_per_solve": f"{args.cpu_sweeps} (a step is {args.cpu_sweeps} "
+                                           f"sweeps; GTEPS counts edge-sweeps)",
+                       "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"},
             "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": "GTEPS", "h2d_bytes_per_step": 0,
@@ -630,9 +837,16 @@ def main():
     L = _ffi.lib()
     stream = torch.cuda.current_stream(device)
     h = C.c_void_p()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     _ffi.check(L.gtc_graph_create_device(n, m, C.c_void_p(src.data_ptr()),
                                          C.c_void_p(tgt.data_ptr()),
                                          C.c_void_p(stream.cuda_stream), C.byref(h)))
+    torch.cuda.synchronize()
+    build = {"ms": 1e3 * (time.perf_counter() - t0),
+             "what": "gtc_graph_create_device: CSR and CSC in the add_edge order of the "
+                     "reference's blocks, relabelled by out-degree (device edge list in)"}
+    build["edges_per_s"] = m / (build["ms"] / 1e3)
     _ffi.check(L.gtc_graph_set_stream(h, C.c_void_p(stream.cuda_stream)))
     if args.section == "adjoint":
         out = adjoint_section(L, h, n, m, device, stream, wl)
@@ -723,6 +937,7 @@ def main():
     # ---- CPU baseline ------------------------------------------------------
     cpu = None
     parity = None
+    extra = {}
     if rank == 0 and world == 1 and not args.no_cpu:
         src_np = src.cpu().numpy().astype(np.uint32)
         tgt_np = tgt.cpu().numpy().astype(np.uint32)
@@ -752,6 +967,16 @@ def main():
                       "reference": "gtc_oracle.c f64 pagerank, same graph, same epsilon"}
         except Exception as e:  # noqa: BLE001  (reported; the headline stands)
             parity = {"error": repr(e)}
+            want = None
+        if not args.no_secondary and args.workload == "rmat24":
+            try:
+                extra["weighted"] = weighted_section(L, h, n, m, device, stream, g, threads)
+            except Exception as e:  # noqa: BLE001
+                extra["weighted"] = {"error": repr(e)}
+            try:
+                extra["exact_f64"] = exact_section(L, h, n, m, device, stream, want)
+            except Exception as e:  # noqa: BLE001
+                extra["exact_f64"] = {"error": repr(e)}
         del g
 
     secondary = {}
@@ -759,7 +984,7 @@ def main():
         for name, fn in (("adjoint", adjoint_section), ("ppr_batch", ppr_section),
                          ("graph_batch", graph_batch_section),
                          ("betweenness", betweenness_section),
-                         ("eigenvector", eigenvector_section)):
+                         ("chunglu", chunglu_section)):
             try:
                 secondary[name] = fn(L, h, n, m, device, stream, wl) if name == "adjoint" else fn(L, device, stream)
             except Exception as e:  # noqa: BLE001  (reported, the headline stands)
@@ -777,8 +1002,9 @@ def main():
                 "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "parity_vs_f64_oracle": parity,
             "gpu_launches": int(launches), "sweep_launches": int(sweep_launches),
-            "clocks": clk.summary(),
+            "clocks": clk.summary(), "build": build,
         }
+        out.update(extra)
         out.update(secondary)
         print(json.dumps(out), flush=True)
     _ffi.check(L.gtc_graph_destroy(h))

@@ -90,22 +90,6 @@ static gtc_graph* new_graph(uint64_t n, uint64_t m) {
         throw Error{GTC_ERR_CUDA, std::string("stream creation failed: ") + cudaGetErrorString(e)};
     }
     g->stream = g->home;
-    // The sizes are stored once more and read back: on GB300 hosts the first
-    // handle of a process was seen to lose the constructor's store of m (it
-    // read 0 right after construction, in heap or mmap'd memory alike),
-    // which turned the first solve into one over an edgeless graph.
-    volatile uint32_t* vn = &g->n;
-    volatile uint32_t* vm = &g->m;
-    for (int k = 0; k < 3 && (*vn != (uint32_t)n || *vm != (uint32_t)m); ++k) {
-        *vn = (uint32_t)n;
-        *vm = (uint32_t)m;
-        __atomic_thread_fence(__ATOMIC_SEQ_CST);
-    }
-    if (*vn != (uint32_t)n || *vm != (uint32_t)m) {
-        cudaStreamDestroy(g->home);
-        delete g;
-        throw Error{GTC_ERR_CUDA, "the graph handle did not keep its sizes (internal error)"};
-    }
     return g;
 }
 
@@ -194,6 +178,22 @@ int gtc_graph_create(uint64_t n, uint64_t m, const uint32_t* src, const uint32_t
     });
 }
 
+int gtc_graph_create_blocks(uint64_t n, uint64_t edge_bound, const uint64_t* block_off,
+                            const uint32_t* out_len, const uint32_t* entries, gtc_graph** out) {
+    return guarded([&] {
+        GTC_REQUIRE(out, GTC_ERR_ARG, "out is NULL");
+        *out = nullptr;
+        gtc_graph* g = new_graph(n, edge_bound);
+        try {
+            build_from_blocks(g, block_off, out_len, entries);
+        } catch (...) {
+            destroy_graph(g);
+            throw;
+        }
+        *out = g;
+    });
+}
+
 int gtc_graph_destroy(gtc_graph* g) {
     return guarded([&] { destroy_graph(g); });
 }
@@ -203,7 +203,7 @@ int gtc_graph_info(const gtc_graph* g, uint64_t* n, uint64_t* edge_bound, uint64
         GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
         if (n) *n = g->n;
         if (edge_bound) *edge_bound = g->m;
-        if (num_edges) *num_edges = g->m;
+        if (num_edges) *num_edges = g->m_live;
     });
 }
 
@@ -212,7 +212,7 @@ int gtc_graph_export(const gtc_graph* g, uint64_t* out_off, uint32_t* out_other,
     return guarded([&] {
         GTC_REQUIRE(g, GTC_ERR_ARG, "graph is NULL");
         cudaStream_t s = g->home;
-        const size_t n = g->n, m = g->m;
+        const size_t n = g->n, m = g->m_live;
         std::vector<uint32_t> perm(n), iperm(n), off(n + 1), other(m), eid(m);
         if (n) GTC_CUDA(cudaMemcpyAsync(perm.data(), g->perm.get(), n * 4, cudaMemcpyDeviceToHost, s));
         GTC_CUDA(cudaStreamSynchronize(s));

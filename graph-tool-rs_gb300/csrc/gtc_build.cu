@@ -502,8 +502,23 @@ void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt, bo
         L += 2;
     }
 
-    // relabel by descending out-degree (stable: ties keep index order); a
-    // packed batch of graphs keeps its labels (each graph stays contiguous)
+    relabel_graph(g, d_src, d_tgt, relabel, &L);
+    GTC_CUDA(cudaStreamSynchronize(s));
+    g->launches += L;
+}
+
+// The relabelling of a graph whose halves are built in original labels:
+// vertices by descending out-degree (stable: ties keep index order), or
+// kept as they are (a packed batch of graphs: each graph stays contiguous),
+// and both halves rewritten in the new labels with every block's order
+// kept.  src_of / tgt_of: the endpoints of every edge id (edge bound
+// entries; ids without an edge are never read).
+void relabel_graph(gtc_graph* g, const uint32_t* src_of, const uint32_t* tgt_of, bool relabel,
+                   uint64_t* Lp) {
+    cudaStream_t s = g->home;
+    const uint32_t n = g->n, m = g->m_live;
+    const unsigned TB = 256;
+    uint64_t& L = *Lp;
     g->perm.alloc(n, s);
     g->iperm.alloc(n, s);
     if (n && !relabel) {
@@ -526,9 +541,83 @@ void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt, bo
         GTC_LAUNCHED();
         L += 3;
     }
-    relabel_half(n, m, g->perm.get(), g->iperm.get(), d_tgt, g->out, s, &L);
-    relabel_half(n, m, g->perm.get(), g->iperm.get(), d_src, g->in, s, &L);
-    GTC_CUDA(cudaStreamSynchronize(s));
+    relabel_half(n, m, g->perm.get(), g->iperm.get(), tgt_of, g->out, s, &L);
+    relabel_half(n, m, g->perm.get(), g->iperm.get(), src_of, g->in, s, &L);
+}
+
+void build_from_blocks(gtc_graph* g, const uint64_t* block_off, const uint32_t* out_len,
+                       const uint32_t* entries) {
+    cudaStream_t s = g->home;
+    const uint32_t n = g->n, eb = g->m;
+    constexpr uint32_t NONE = 0xFFFFFFFFu;
+    uint64_t L = 0;
+    // ---- the blocks, split into their halves, checked on the host ----
+    GTC_REQUIRE(n == 0 || (block_off && out_len), GTC_ERR_ARG, "block_off / out_len is NULL");
+    GTC_REQUIRE(n == 0 || block_off[0] == 0, GTC_ERR_ARG, "block_off[0] must be 0");
+    uint64_t mo = 0, mi = 0;
+    for (uint32_t v = 0; v < n; ++v) {
+        GTC_REQUIRE(block_off[v + 1] >= block_off[v], GTC_ERR_ARG, "block offsets must not decrease");
+        const uint64_t len = block_off[v + 1] - block_off[v];
+        GTC_REQUIRE(out_len[v] <= len, GTC_ERR_ARG, "a block's out_len exceeds its length");
+        mo += out_len[v];
+        mi += len - out_len[v];
+    }
+    GTC_REQUIRE(mo == mi, GTC_ERR_ARG,
+                "the blocks hold a different number of out-entries and in-entries");
+    GTC_REQUIRE(mo <= eb, GTC_ERR_ARG, "more live edges than the edge bound");
+    GTC_REQUIRE(mo == 0 || entries, GTC_ERR_ARG, "entries is NULL");
+    const uint32_t m = (uint32_t)mo;
+    g->m_live = m;
+    std::vector<uint32_t> src_of(eb, NONE), tgt_of(eb, NONE);
+    std::vector<uint32_t> oo((size_t)n + 1), io((size_t)n + 1), oth(m), oid(m), ith(m), iid(m);
+    uint64_t po = 0;
+    for (uint32_t v = 0; v < n; ++v) {  // out-halves: (target, id) in storage order
+        oo[v] = (uint32_t)po;
+        for (uint64_t k = block_off[v], e = block_off[v] + out_len[v]; k < e; ++k, ++po) {
+            const uint32_t t = entries[2 * k], id = entries[2 * k + 1];
+            GTC_REQUIRE(t < n, GTC_ERR_INDEX, "a block entry names a vertex >= n");
+            GTC_REQUIRE(id < eb, GTC_ERR_INDEX, "a block entry names an edge id >= edge_bound");
+            GTC_REQUIRE(src_of[id] == NONE, GTC_ERR_ARG, "an edge id appears in two out-halves");
+            src_of[id] = v;
+            tgt_of[id] = t;
+            oth[po] = t;
+            oid[po] = id;
+        }
+    }
+    oo[n] = (uint32_t)po;
+    std::vector<uint8_t> seen(eb, 0);
+    uint64_t pi = 0;
+    for (uint32_t v = 0; v < n; ++v) {  // in-halves: (source, id) in storage order
+        io[v] = (uint32_t)pi;
+        for (uint64_t k = block_off[v] + out_len[v], e = block_off[v + 1]; k < e; ++k, ++pi) {
+            const uint32_t src = entries[2 * k], id = entries[2 * k + 1];
+            GTC_REQUIRE(src < n, GTC_ERR_INDEX, "a block entry names a vertex >= n");
+            GTC_REQUIRE(id < eb, GTC_ERR_INDEX, "a block entry names an edge id >= edge_bound");
+            GTC_REQUIRE(src_of[id] == src && tgt_of[id] == v && !seen[id], GTC_ERR_ARG,
+                        "an in-entry does not match its edge's out-entry");
+            seen[id] = 1;
+            ith[pi] = src;
+            iid[pi] = id;
+        }
+    }
+    io[n] = (uint32_t)pi;
+    // ---- to the device, then the relabelling every handle gets ----
+    auto up = [&](DevBuf<uint32_t>& d, const std::vector<uint32_t>& h) {
+        d.alloc(h.size(), s);
+        if (!h.empty())
+            GTC_CUDA(cudaMemcpyAsync(d.get(), h.data(), h.size() * 4, cudaMemcpyHostToDevice, s));
+    };
+    up(g->out.off, oo);
+    up(g->out.other, oth);
+    up(g->out.eid, oid);
+    up(g->in.off, io);
+    up(g->in.other, ith);
+    up(g->in.eid, iid);
+    DevBuf<uint32_t> dso, dto;
+    up(dso, src_of);
+    up(dto, tgt_of);
+    relabel_graph(g, dso.get(), dto.get(), true, &L);
+    GTC_CUDA(cudaStreamSynchronize(s));  // the host vectors die here
     g->launches += L;
 }
 

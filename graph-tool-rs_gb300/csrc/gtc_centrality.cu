@@ -20,61 +20,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <utility>
+#include <vector>
 
 #include "gtc_sweep.cuh"
 #include "gtc_view.cuh"
 
 namespace gtc {
-
-// --------------------------------------------------------------------------
-// deterministic block reduction of two FP64 partials + last-block fold
-// --------------------------------------------------------------------------
-
-struct Fold2 {
-    double* part_a;    // [gridDim.x]
-    double* part_b;    // [gridDim.x]
-    unsigned* ticket;  // zero before the launch; the last block resets it
-    double* out_a;     // folded results
-    double* out_b;
-};
-
-// Block of NT threads; every thread passes its (a, b).  The last block to
-// finish folds all block partials in block order.
-template <int NT>
-__device__ __forceinline__ void block_fold2(double a, double b, const Fold2& f) {
-    __shared__ double sa[NT / 32], sb[NT / 32];
-    __shared__ bool last;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    a = warp_sum_f64(a);
-    b = warp_sum_f64(b);
-    if (lane == 0) sa[warp] = a, sb[warp] = b;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double ta = 0.0, tb = 0.0;
-        for (int w = 0; w < NT / 32; ++w) ta += sa[w], tb += sb[w];
-        f.part_a[blockIdx.x] = ta;
-        f.part_b[blockIdx.x] = tb;
-        __threadfence();
-        unsigned t = atomicAdd(f.ticket, 1u);
-        last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (last && warp == 0) {
-        __threadfence();
-        double ta = 0.0, tb = 0.0;
-        for (unsigned i = lane; i < gridDim.x; i += 32) {
-            ta += __ldcg(f.part_a + i);
-            tb += __ldcg(f.part_b + i);
-        }
-        ta = warp_sum_f64(ta);
-        tb = warp_sum_f64(tb);
-        if (lane == 0) {
-            *f.out_a = ta;
-            *f.out_b = tb;
-            *f.ticket = 0u;
-        }
-    }
-}
 
 constexpr int PR_NT = 256;
 
@@ -198,19 +150,19 @@ __global__ void k_store(uint32_t n, const uint32_t* __restrict__ iperm, const T*
         ((float*)x)[v] = (float)val;
 }
 
-// y = rank * invdeg, plus the dangling mass of rank (block-folded).
+// y = rank * invdeg, plus the dangling mass of rank (summed exactly).
 __global__ void __launch_bounds__(PR_NT) k_pr_prime(uint32_t n, const float* __restrict__ r,
                                                    const float* __restrict__ invdeg,
                                                    const uint8_t* __restrict__ sink,
-                                                   float* __restrict__ y, Fold2 f) {
-    Kahan sacc;
+                                                   float* __restrict__ y, ExactFold f) {
+    ExactPR none, sacc;
     for (size_t v = (size_t)blockIdx.x * PR_NT + threadIdx.x; v < n;
          v += (size_t)gridDim.x * PR_NT) {
         float x = r[v];
         y[v] = __fmul_rn(x, invdeg[v]);
         if (sink[v]) sacc.add(x);
     }
-    block_fold2<PR_NT>(0.0, (double)sacc.s + (double)sacc.c, f);
+    block_fold_exact<PR_NT>(none, sacc, f);
 }
 
 // --------------------------------------------------------------------------
@@ -226,6 +178,22 @@ __device__ __forceinline__ void plan_range(uint64_t n, uint64_t chunks, uint64_t
 }
 
 // One thread per row, the in-edge loop sequential in storage order.
+// Rows of more than F64_SHORT entries are summed by a warp (k_pr_f64_long,
+// k_ev_f64_long); shorter rows by a thread each.
+constexpr uint32_t F64_SHORT = 32;
+
+// acc + t(lane 0) + t(lane 1) + ... + t(lane 31), left to right, skipping the
+// lanes whose bit of `valid` is clear: the sequential fold of 32 terms the
+// lanes computed in parallel.  Every lane ends with the same acc.
+__device__ __forceinline__ double fold_lanes_in_order(double acc, double t, unsigned valid) {
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+        const double tk = __shfl_sync(0xffffffffu, t, k);
+        if ((valid >> k) & 1u) acc = __dadd_rn(acc, tk);
+    }
+    return acc;
+}
+
 __global__ void k_pr_f64_rows(uint32_t n, const uint32_t* __restrict__ off,
                               const uint32_t* __restrict__ other, const double* __restrict__ w,
                               const double* __restrict__ deg, const uint8_t* __restrict__ active,
@@ -235,6 +203,7 @@ __global__ void k_pr_f64_rows(uint32_t n, const uint32_t* __restrict__ off,
                               double* __restrict__ diff) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (off[i + 1] - off[i] > F64_SHORT) return;  // k_pr_f64_long's
     if (active && !active[i]) {
         next[i] = prev[i];
         diff[i] = 0.0;
@@ -256,25 +225,81 @@ __global__ void k_pr_f64_rows(uint32_t n, const uint32_t* __restrict__ off,
     next[i] = nv;
 }
 
-// Plan-chunk partials: thread k folds its chunk sequentially from 0.0.
+// The rows k_pr_f64_rows leaves (more than F64_SHORT entries): a warp per
+// row.  Lanes gather and form 32 terms (prev[s] * w) / ds at a time; the
+// terms are then added to r one after the other in entry order, as the
+// reference's loop does, so r has the same bits.
+__global__ void k_pr_f64_long(uint32_t n, const uint32_t* __restrict__ off,
+                              const uint32_t* __restrict__ other, const double* __restrict__ w,
+                              const double* __restrict__ deg, const uint8_t* __restrict__ active,
+                              const double* __restrict__ pers, double uniform, double one_minus_d,
+                              double d, const double* __restrict__ psink_p,
+                              const double* __restrict__ prev, double* __restrict__ next,
+                              double* __restrict__ diff) {
+    const unsigned lane = threadIdx.x & 31;
+    const size_t warps = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t i = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const uint32_t b = off[i], e = off[i + 1];
+        if (e - b <= F64_SHORT) continue;
+        if (active && !active[i]) {
+            if (lane == 0) next[i] = prev[i], diff[i] = 0.0;
+            continue;
+        }
+        const double pv = pers ? pers[i] : uniform;
+        double r = __dmul_rn(*psink_p, pv);
+        for (uint32_t base = b; base < e; base += 32) {
+            const uint32_t p = base + lane;
+            double t = 0.0;
+            bool ok = false;
+            if (p < e) {
+                const uint32_t src = other[p];
+                const double ds = deg[src];
+                if (ds != 0.0) {
+                    t = __ddiv_rn(__dmul_rn(prev[src], w ? w[p] : 1.0), ds);
+                    ok = true;
+                }
+            }
+            r = fold_lanes_in_order(r, t, __ballot_sync(0xffffffffu, ok));
+        }
+        if (lane == 0) {
+            const double nv = __dadd_rn(__dmul_rn(one_minus_d, pv), __dmul_rn(d, r));
+            diff[i] = fabs(__dsub_rn(nv, prev[i]));
+            next[i] = nv;
+        }
+    }
+}
+
+// Plan-chunk partials: a warp per chunk folds it sequentially from 0.0
+// (lanes load 32 values at a time; the adds run in index order).
 __global__ void k_chunk_sums(uint64_t n, uint64_t chunks, const double* __restrict__ v,
                              const uint32_t* __restrict__ gather, double* __restrict__ part) {
-    uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= chunks) return;
+    const unsigned lane = threadIdx.x & 31;
+    const uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (k >= chunks) return;  // whole warps leave together
     uint64_t s, e;
     plan_range(n, chunks, k, s, e);
     double acc = 0.0;
-    for (uint64_t i = s; i < e; ++i) acc = __dadd_rn(acc, gather ? v[gather[i]] : v[i]);
-    part[k] = acc;
+    for (uint64_t base = s; base < e; base += 32) {
+        const uint64_t i = base + lane;
+        const bool ok = i < e;
+        const double t = ok ? (gather ? v[gather[i]] : v[i]) : 0.0;
+        acc = fold_lanes_in_order(acc, t, __ballot_sync(0xffffffffu, ok));
+    }
+    if (lane == 0) part[k] = acc;
 }
 
-// Left fold of the chunk partials from 0.0 (one thread).  mode 0: out = sum;
+// Left fold of the chunk partials from 0.0 (one warp, adds in order).  mode 0: out = sum;
 // mode 1: out = sum and out2 = the eigenvector scale (sqrt, 1 if zero).
 __global__ void k_fold(uint64_t chunks, const double* __restrict__ part, double* out,
                        double* out2, int mode) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const unsigned lane = threadIdx.x;
     double acc = 0.0;
-    for (uint64_t k = 0; k < chunks; ++k) acc = __dadd_rn(acc, part[k]);
+    for (uint64_t base = 0; base < chunks; base += 32) {
+        const bool ok = base + lane < chunks;
+        acc = fold_lanes_in_order(acc, ok ? part[base + lane] : 0.0, __ballot_sync(0xffffffffu, ok));
+    }
+    if (lane != 0) return;
     *out = acc;
     if (mode == 1) {
         double norm = __dsqrt_rn(acc);
@@ -307,6 +332,7 @@ __global__ void k_ev_f64_rows(uint32_t n, const uint32_t* __restrict__ off,
                               double* __restrict__ next, double* __restrict__ sq) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (off[i + 1] - off[i] > F64_SHORT) return;  // k_ev_f64_long's
     if (active && !active[i]) {
         next[i] = prev[i];
         sq[i] = 0.0;
@@ -319,6 +345,35 @@ __global__ void k_ev_f64_rows(uint32_t n, const uint32_t* __restrict__ off,
     }
     next[i] = s;
     sq[i] = __dmul_rn(s, s);
+}
+
+// The rows k_ev_f64_rows leaves: a warp per row, terms w * prev[other]
+// formed 32 at a time and added in entry order.
+__global__ void k_ev_f64_long(uint32_t n, const uint32_t* __restrict__ off,
+                              const uint32_t* __restrict__ other, const double* __restrict__ w,
+                              const uint8_t* __restrict__ active, const double* __restrict__ prev,
+                              double* __restrict__ next, double* __restrict__ sq) {
+    const unsigned lane = threadIdx.x & 31;
+    const size_t warps = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t i = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const uint32_t b = off[i], e = off[i + 1];
+        if (e - b <= F64_SHORT) continue;
+        if (active && !active[i]) {
+            if (lane == 0) next[i] = prev[i], sq[i] = 0.0;
+            continue;
+        }
+        double s = 0.0;
+        for (uint32_t base = b; base < e; base += 32) {
+            const uint32_t p = base + lane;
+            const bool ok = p < e;
+            const double t = ok ? __dmul_rn(w ? w[p] : 1.0, prev[other[p]]) : 0.0;
+            s = fold_lanes_in_order(s, t, __ballot_sync(0xffffffffu, ok));
+        }
+        if (lane == 0) {
+            next[i] = s;
+            sq[i] = __dmul_rn(s, s);
+        }
+    }
 }
 
 // Eigenvector sweep 2 (centrality.rs:472-484): next /= scale, |next - prev|.
@@ -340,7 +395,8 @@ __global__ void k_ev_f64_norm(uint32_t n, const uint8_t* __restrict__ active,
 // FP32 eigenvector
 // --------------------------------------------------------------------------
 
-// next /= scale (scale from the FP64 norm, 1 if zero) and the FP64 delta.
+// next /= scale (scale from the FP64 norm, 1 if zero) and the L1 change,
+// summed exactly.
 // The FP64 reciprocal is applied as an unevaluated sum hi + lo of two floats,
 // so the stored value is (nearly always) the correctly rounded s / norm: a
 // last-bit change of the norm between sweeps does not move every entry by an
@@ -349,12 +405,13 @@ __global__ void __launch_bounds__(PR_NT) k_ev_f32_norm(uint32_t n,
                                                       const uint8_t* __restrict__ active,
                                                       const double* __restrict__ sqnorm,
                                                       const float* __restrict__ prev,
-                                                      float* __restrict__ next, Fold2 f) {
+                                                      float* __restrict__ next, ExactFold f) {
+    if (f.stop && *f.stop) return;  // the iteration has stopped (same for every CTA)
     const double norm = sqrt(*sqnorm);
     const double inv = 1.0 / (norm == 0.0 ? 1.0 : norm);
     const float ih = (float)inv;
     const float il = (float)(inv - (double)ih);
-    Kahan dacc;
+    ExactPR dacc, none;
     for (size_t v = (size_t)blockIdx.x * PR_NT + threadIdx.x; v < n;
          v += (size_t)gridDim.x * PR_NT) {
         if (active && !active[v]) continue;
@@ -363,7 +420,7 @@ __global__ void __launch_bounds__(PR_NT) k_ev_f32_norm(uint32_t n,
         next[v] = x;
         dacc.add(fabsf(__fsub_rn(x, prev[v])));
     }
-    block_fold2<PR_NT>((double)dacc.s + (double)dacc.c, 0.0, f);
+    block_fold_exact<PR_NT>(dacc, none, f);
 }
 
 // --------------------------------------------------------------------------
@@ -394,24 +451,80 @@ struct Timer {
     }
 };
 
-// Reduction scratch for one launch shape.
+// Reduction scratch of one exactly-folded launch (at most FOLD_MAX_CTAS CTAs).
 struct FoldBufs {
-    DevBuf<double> pa, pb, out;
+    DevBuf<uint4> part;
+    DevBuf<double> out;
     DevBuf<unsigned> ticket;
     FoldBufs(unsigned blocks, cudaStream_t s)
-        : pa(blocks, s), pb(blocks, s), out(4, s), ticket(1, s) {
+        : part(2 * (size_t)std::max(blocks, 1u), s), out(4, s), ticket(1, s) {
+        GTC_REQUIRE(blocks <= FOLD_MAX_CTAS, GTC_ERR_ARG, "grid exceeds the fold capacity");
         GTC_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), s));
         GTC_CUDA(cudaMemsetAsync(out.get(), 0, 4 * sizeof(double), s));
     }
-    Fold2 fold(double* oa, double* ob) { return Fold2{pa.get(), pb.get(), ticket.get(), oa, ob}; }
+    ExactFold fold(double* oa, double* ob) { return ExactFold{part.get(), ticket.get(), oa, ob}; }
 };
 
 unsigned persistent_blocks(uint32_t rows) {
     // one row per warp, at most 8 resident blocks of 256 threads per SM
     unsigned want = (rows + (PR_NT / 32) - 1) / (PR_NT / 32);
-    unsigned cap = (unsigned)sm_count() * 8;
+    unsigned cap = std::min<unsigned>((unsigned)sm_count() * 8, FOLD_MAX_CTAS);
     return want < 1 ? 1 : (want > cap ? cap : want);
 }
+
+// Sweeps a host loop enqueues between two reads of the device-side stop
+// flag: a sweep after the stop returns at once, so at most STOP_BATCH - 1
+// launches are wasted, against one host round trip per sweep saved.
+constexpr int STOP_BATCH = 8;
+
+// Device-side state of a power iteration's stop (ExactFold::stop/iters).
+struct StopState {
+    DevBuf<unsigned long long> words;  // [0] stop flag, [1] sweeps done
+    explicit StopState(cudaStream_t s) : words(2, s) {
+        GTC_CUDA(cudaMemsetAsync(words.get(), 0, 2 * sizeof(unsigned long long), s));
+    }
+    unsigned* stop() { return reinterpret_cast<unsigned*>(words.get()); }
+    unsigned long long* iters() { return words.get() + 1; }
+    void arm(ExactFold& f, double eps, uint64_t max_iter) {
+        f.stop = stop();
+        f.iters = iters();
+        f.eps = eps;
+        f.max_iter = max_iter;
+    }
+    // (stop flag, sweeps done), after the stream has reached this point
+    std::pair<bool, uint64_t> read(cudaStream_t s) {
+        unsigned long long h[2] = {0, 0};
+        GTC_CUDA(cudaMemcpyAsync(h, words.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+        return {(h[0] & 0xFFFFFFFFull) != 0, h[1]};
+    }
+};
+
+// Per-launch CUDA events of the sweeps of a batched loop; only the sweeps
+// that ran (the first `done`) are summed.
+struct SweepEvents {
+    std::vector<cudaEvent_t> ev;
+    ~SweepEvents() {
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    }
+    void record(cudaStream_t s) {
+        cudaEvent_t e = nullptr;
+        GTC_CUDA(cudaEventCreate(&e));
+        ev.push_back(e);
+        GTC_CUDA(cudaEventRecord(e, s));
+    }
+    // events come in (start, stop) pairs, one pair per launch
+    double ms(uint64_t done) {
+        double t = 0.0;
+        for (uint64_t k = 0; k < done && 2 * k + 1 < ev.size(); ++k) {
+            GTC_CUDA(cudaEventSynchronize(ev[2 * k + 1]));
+            float x = 0.f;
+            GTC_CUDA(cudaEventElapsedTime(&x, ev[2 * k], ev[2 * k + 1]));
+            t += x;
+        }
+        return t;
+    }
+};
 
 // The pull schedule of a view: cached on the graph for the plain and the
 // reversed view, cut per call for a filtered one.
@@ -472,7 +585,7 @@ VariantShape variant_shape(uint32_t n_units, uint32_t hot_n) {
                                                                NT, dyn_max));
         if (per_sm < 1) per_sm = 1;
     }
-    const unsigned cap = (unsigned)(per_sm * sms);
+    const unsigned cap = std::min<unsigned>((unsigned)(per_sm * sms), FOLD_MAX_CTAS);
     const unsigned want = (n_units + NT / 32 - 1) / (NT / 32);
     VariantShape v;
     v.grid = want < 1 ? 1u : (want < cap ? want : cap);
@@ -555,8 +668,6 @@ void set_schedule(SweepArgs& A, const Units& u, const View& view) {
     A.sidx = u.sidx.get();
     A.partial = u.partial.get();
     A.counter = u.counter.get();
-    A.long_out = u.long_out.get();
-    A.item_out = u.item_out.get();
     A.n_units = u.n_units;
     A.n_long = u.n_long;
     A.off = view.pull_off;
@@ -720,21 +831,25 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         total.start();
         while (delta >= eps) {
             if (in.timing) sw.start();
-            k_chunk_sums<<<grid_for(sink_chunks, 128, 1u << 30), 128, 0, s>>>(
+            k_chunk_sums<<<grid_for(sink_chunks * 32, 128, 1u << 30), 128, 0, s>>>(
                 n_sinks, sink_chunks, cur, sinks.get(), part.get());
             k_fold<<<1, 32, 0, s>>>(sink_chunks, part.get(), scal.get(), nullptr, 0);
-            if (n)
+            if (n) {
                 k_pr_f64_rows<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(
                     n, view.pull_off, view.pull_other, wpull.get(), P.deg.get(), act, pers64,
                     P.uniform, 1.0 - d, d, scal.get(), cur, nxt, diff.get());
+                k_pr_f64_long<<<(unsigned)sm_count() * 8, 256, 0, s>>>(
+                    n, view.pull_off, view.pull_other, wpull.get(), P.deg.get(), act, pers64,
+                    P.uniform, 1.0 - d, d, scal.get(), cur, nxt, diff.get());
+            }
             // the delta is folded over the Plan in original vertex order
-            k_chunk_sums<<<grid_for(chunks, 128, 1u << 30), 128, 0, s>>>(n, chunks, diff.get(),
+            k_chunk_sums<<<grid_for(chunks * 32, 128, 1u << 30), 128, 0, s>>>(n, chunks, diff.get(),
                                                                          g->iperm.get(), part.get());
             k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get() + 1, nullptr, 0);
             GTC_LAUNCHED();
             if (in.timing) sw.stop();
-            L += n ? 5 : 4;
-            SL += n ? 5 : 4;
+            L += n ? 6 : 4;
+            SL += n ? 6 : 4;
             GTC_CUDA(cudaMemcpyAsync(&delta, scal.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
             GTC_CUDA(cudaStreamSynchronize(s));
             if (in.timing) sweep_ms += sw.ms();
@@ -802,30 +917,42 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         A.one_minus_d = (float)(1.0 - d);
         A.d = (float)d;
         A.psink = dq + 1;
-        A.ticket = fs.ticket.get();
-        A.out = dq;
+        A.fold = ExactFold{U->fold_part.get(), fs.ticket.get(), dq, dq + 1};
         A.x = yc, A.prev = rc, A.next = rn, A.ynext = yn;
         const int var = tuned_variant<MODE_PAGERANK>(*U, A, W, in.schedule, s, &L);
         // a tuning trial wrote the dangling mass of its output: restore it
         GTC_CUDA(cudaMemcpyAsync(dq + 1, dp + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
+        // The loop of centrality.rs:318-376 with the stop decided on the
+        // device: sweeps go out in batches and the host reads the stop flag
+        // once a batch (a sweep after the stop returns at once).
+        StopState st(s);
+        st.arm(A.fold, eps, max_iter);
+        A.stop = st.stop();
+        SweepEvents evs;
+        float* rb[2] = {rc, rn};
+        float* ybuf[2] = {yc, yn};
+        uint64_t launched = 0;
         total.start();
-        while (delta >= eps) {
-            A.x = yc, A.prev = rc, A.next = rn, A.ynext = yn;
-            if (in.timing) sw.start();
-            launch_sweep<MODE_PAGERANK>(var, A, W, s);
-            if (in.timing) sw.stop();
-            L++;
-            SL++;
-            GTC_CUDA(cudaMemcpyAsync(&delta, dq, sizeof(double), cudaMemcpyDeviceToHost, s));
-            GTC_CUDA(cudaStreamSynchronize(s));
-            if (in.timing) sweep_ms += sw.ms();
-            std::swap(rc, rn);
-            std::swap(yc, yn);
-            iter++;
-            if (max_iter > 0 && iter == max_iter) break;
+        for (bool stopped = false; !stopped;) {
+            for (int k = 0; k < STOP_BATCH; ++k, ++launched) {
+                const int c = (int)(launched & 1);
+                A.x = ybuf[c], A.prev = rb[c], A.next = rb[c ^ 1], A.ynext = ybuf[c ^ 1];
+                if (in.timing) evs.record(s);
+                launch_sweep<MODE_PAGERANK>(var, A, W, s);
+                if (in.timing) evs.record(s);
+                L++;
+                SL++;
+            }
+            const auto rs = st.read(s);
+            stopped = rs.first;
+            iter = rs.second;
         }
         total.stop();
+        GTC_CUDA(cudaMemcpyAsync(&delta, dq, sizeof(double), cudaMemcpyDeviceToHost, s));
         res->device_ms = total.ms();
+        if (in.timing) sweep_ms = evs.ms(iter);
+        SL = iter;
+        rc = rb[iter & 1];
         store_result<float>(g, n, rc, P, in, s, &L);
     }
     GTC_CUDA(cudaStreamSynchronize(s));
@@ -860,23 +987,26 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         total.start();
         while (delta >= eps) {
             if (in.timing) sw.start();
-            if (n)
+            if (n) {
                 k_ev_f64_rows<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(
                     n, view.pull_off, view.pull_other, wpull.get(), act, cur, nxt, tmp.get());
-            k_chunk_sums<<<grid_for(chunks, 128, 1u << 30), 128, 0, s>>>(n, chunks, tmp.get(),
+                k_ev_f64_long<<<(unsigned)sm_count() * 8, 256, 0, s>>>(
+                    n, view.pull_off, view.pull_other, wpull.get(), act, cur, nxt, tmp.get());
+            }
+            k_chunk_sums<<<grid_for(chunks * 32, 128, 1u << 30), 128, 0, s>>>(n, chunks, tmp.get(),
                                                                          g->iperm.get(), part.get());
             // scal[0] = squared norm, scal[1] = norm, scal[2] = scale
             k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get(), scal.get() + 2, 1);
             if (n)
                 k_ev_f64_norm<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(n, act, scal.get() + 2,
                                                                          cur, nxt, tmp.get());
-            k_chunk_sums<<<grid_for(chunks, 128, 1u << 30), 128, 0, s>>>(n, chunks, tmp.get(),
+            k_chunk_sums<<<grid_for(chunks * 32, 128, 1u << 30), 128, 0, s>>>(n, chunks, tmp.get(),
                                                                          g->iperm.get(), part.get());
             k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get() + 3, nullptr, 0);
             GTC_LAUNCHED();
             if (in.timing) sw.stop();
-            L += n ? 6 : 4;
-            SL += n ? 6 : 4;
+            L += n ? 7 : 4;
+            SL += n ? 7 : 4;
             double hs[4];
             GTC_CUDA(cudaMemcpyAsync(hs, scal.get(), 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
             GTC_CUDA(cudaStreamSynchronize(s));
@@ -915,32 +1045,43 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         A.sw = swt.get();
         A.w = wpull.get();
         A.active = act;
-        A.ticket = f1.ticket.get();
-        A.out = o1;
+        A.fold = ExactFold{U->fold_part.get(), f1.ticket.get(), o1, o1 + 1};
         A.x = xc, A.prev = xc, A.next = xn;
         const int var = tuned_variant<MODE_EIGEN>(*U, A, W, in.schedule, s, &L);
+        // the loop of centrality.rs:440-492, stopped on the device (as PageRank)
+        StopState st(s);
+        ExactFold fn = f2.fold(o2, o2 + 1);
+        st.arm(fn, eps, max_iter);
+        A.stop = st.stop();
+        SweepEvents evs;
+        float* xb[2] = {xc, xn};
+        uint64_t launched = 0;
         total.start();
-        while (delta >= eps) {
-            A.x = xc, A.prev = xc, A.next = xn;
-            if (in.timing) sw.start();
-            launch_sweep<MODE_EIGEN>(var, A, W, s);
-            k_ev_f32_norm<<<nb, PR_NT, 0, s>>>(n, act, o1, xc, xn, f2.fold(o2, o2 + 1));
-            GTC_LAUNCHED();
-            if (in.timing) sw.stop();
-            L += 2;
-            SL += 2;
-            double sq = 0.0;
-            GTC_CUDA(cudaMemcpyAsync(&sq, o1, sizeof(double), cudaMemcpyDeviceToHost, s));
-            GTC_CUDA(cudaMemcpyAsync(&delta, o2, sizeof(double), cudaMemcpyDeviceToHost, s));
-            GTC_CUDA(cudaStreamSynchronize(s));
-            if (in.timing) sweep_ms += sw.ms();
-            norm = std::sqrt(sq);
-            std::swap(xc, xn);
-            iter++;
-            if (max_iter > 0 && iter == max_iter) break;
+        for (bool stopped = false; !stopped;) {
+            for (int k = 0; k < STOP_BATCH; ++k, ++launched) {
+                const int c = (int)(launched & 1);
+                A.x = xb[c], A.prev = xb[c], A.next = xb[c ^ 1];
+                if (in.timing) evs.record(s);
+                launch_sweep<MODE_EIGEN>(var, A, W, s);
+                k_ev_f32_norm<<<nb, PR_NT, 0, s>>>(n, act, o1, xb[c], xb[c ^ 1], fn);
+                GTC_LAUNCHED();
+                if (in.timing) evs.record(s);
+                L += 2;
+            }
+            const auto rs = st.read(s);
+            stopped = rs.first;
+            iter = rs.second;
         }
         total.stop();
+        double sq = 0.0;
+        GTC_CUDA(cudaMemcpyAsync(&sq, o1, sizeof(double), cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaMemcpyAsync(&delta, o2, sizeof(double), cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+        norm = iter ? std::sqrt(sq) : 0.0;
         res->device_ms = total.ms();
+        if (in.timing) sweep_ms = evs.ms(iter);
+        SL = 2 * iter;
+        xc = xb[iter & 1];
         store_result<float>(g, n, xc, P, in, s, &L);
     }
     GTC_CUDA(cudaStreamSynchronize(s));
@@ -982,20 +1123,20 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
 // the shifted iterate falls below epsilon * |g|_1.
 
 // (sum_v a_v x_v, sum_v b_v y_v) over n entries: a null a or b is the
-// constant ua / ub, a null x or y is 1; `absy` sums |b_v y_v|.  Deterministic
-// block fold into (out_a, out_b).
+// constant ua / ub, a null x or y is 1; `absy` sums |b_v y_v|.  Summed
+// exactly into (out_a, out_b).
 __global__ void __launch_bounds__(PR_NT) k_dot2(uint32_t n, const float* __restrict__ a, float ua,
                                                const float* __restrict__ x,
                                                const float* __restrict__ b, float ub,
-                                               const float* __restrict__ y, bool absy, Fold2 f) {
-    Kahan ka, kb;
+                                               const float* __restrict__ y, bool absy, ExactFold f) {
+    ExactPR ka, kb;
     for (size_t v = (size_t)blockIdx.x * PR_NT + threadIdx.x; v < n;
          v += (size_t)gridDim.x * PR_NT) {
         ka.add(__fmul_rn(a ? a[v] : ua, x ? x[v] : 1.f));
         const float t = __fmul_rn(b ? b[v] : ub, y ? y[v] : 1.f);
         kb.add(absy ? fabsf(t) : t);
     }
-    block_fold2<PR_NT>((double)ka.s + (double)ka.c, (double)kb.s + (double)kb.c, f);
+    block_fold_exact<PR_NT>(ka, kb, f);
 }
 
 // grad_p[v] = (lambda + alpha)[iperm v] * c (original labels)
@@ -1151,8 +1292,7 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     A.psink = dq + 1;  // read but unused in this mode
     A.alpha = (float)alpha;
     A.tau = (float)tau;
-    A.ticket = fs.ticket.get();
-    A.out = dq;
+    A.fold = ExactFold{U->fold_part.get(), fs.ticket.get(), dq, dq + 1};
     A.ynext = atl.get();
     float *lc = lam0.get(), *ln = lam1.get();
     A.x = lc, A.prev = lc, A.next = ln;

@@ -112,8 +112,7 @@ struct Units {
     DevBuf<uint4> longs;         // per long row: {row, first chunk slot, chunks, 0}
     DevBuf<float2> partial;      // per long chunk: compensated partial (s, c)
     DevBuf<unsigned> counter;    // per long row: chunks done (reset by the last)
-    DevBuf<double2> long_out;    // per long row: its epilogue's reduction terms
-    DevBuf<double2> item_out;    // per work item: its rows' reduction terms
+    DevBuf<uint4> fold_part;     // per CTA of a sweep: its exact (a, b) partials
     DevBuf<uint32_t> med;        // medium rows
     DevBuf<uint32_t> slice_rows; // 32 rows per slice (NO_ROW pads)
     DevBuf<uint32_t> slice_off;  // first sliced entry of each slice, n_slices + 1
@@ -207,10 +206,11 @@ struct gtc_graph_batch {
 
 struct gtc_graph {
     gtc_graph() = default;
-    gtc_graph(uint32_t n_, uint32_t m_) : n(n_), m(m_) {}
+    gtc_graph(uint32_t n_, uint32_t m_) : n(n_), m(m_), m_live(m_) {}
     int device = 0;
-    uint32_t n = 0;  // vertex bound
-    uint32_t m = 0;  // edge bound == live edges (ids 0..m-1)
+    uint32_t n = 0;       // vertex bound
+    uint32_t m = 0;       // edge bound: edge ids are below it (weight maps hold m entries)
+    uint32_t m_live = 0;  // live edges: the entries of each half (m unless ids have holes)
     cudaStream_t home = nullptr;    // owned; graph-lifetime buffers live on it
     cudaStream_t stream = nullptr;  // where solves run (home, or the caller's)
     // Internally vertices are relabelled by descending out-degree (ties by
@@ -231,6 +231,11 @@ namespace gtc {
 // graph build (gtc_build.cu)
 void build_halves(gtc_graph* g, const uint32_t* d_src, const uint32_t* d_tgt, bool relabel = true);
 void build_schedule(gtc_graph* g, bool in_dir, uint32_t cap);
+// A graph from the reference's blocks as stored (gtc_graph_create_blocks).
+void build_from_blocks(gtc_graph* g, const uint64_t* block_off, const uint32_t* out_len,
+                       const uint32_t* entries);
+void relabel_graph(gtc_graph* g, const uint32_t* src_of, const uint32_t* tgt_of, bool relabel,
+                   uint64_t* launches);
 
 // A device vector of either float type.
 struct DVec {
@@ -393,6 +398,171 @@ __device__ __forceinline__ void warp_merge_kahan(Kahan& k) {
         float os = __shfl_xor_sync(0xffffffffu, k.s, o);
         float oc = __shfl_xor_sync(0xffffffffu, k.c, o);
         k.merge(os, oc);
+    }
+}
+
+// Exact sum of FP32 terms in 128-bit fixed point: the value is X * 2^-FRAC
+// with X a two's-complement integer in four 32-bit words (w0 lowest).  A
+// term x is added as the integer m * 2^(e - 150 + FRAC) (m the 24-bit
+// significand, e the biased exponent), which is exact for |x| >= 2^(23 -
+// FRAC) and truncated toward zero below; |x| must stay below 2^(127 -
+// FRAC).  Integer addition is associative, so a sum does not depend on
+// the order of its terms or on how partial sums are grouped: every thread,
+// warp and CTA schedule gives the same bits.  The words add with the
+// carry chain of add.cc/addc (no FP64 pipe, which is slow on this GPU).
+template <int FRAC>
+struct Exact128 {
+    uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u;
+
+    __device__ __forceinline__ void add_words(uint32_t t0, uint32_t t1, uint32_t t2, uint32_t t3) {
+        asm("add.cc.u32 %0, %0, %4;\n\t"
+            "addc.cc.u32 %1, %1, %5;\n\t"
+            "addc.cc.u32 %2, %2, %6;\n\t"
+            "addc.u32 %3, %3, %7;"
+            : "+r"(w0), "+r"(w1), "+r"(w2), "+r"(w3)
+            : "r"(t0), "r"(t1), "r"(t2), "r"(t3));
+    }
+    __device__ __forceinline__ void sub_words(uint32_t t0, uint32_t t1, uint32_t t2, uint32_t t3) {
+        asm("sub.cc.u32 %0, %0, %4;\n\t"
+            "subc.cc.u32 %1, %1, %5;\n\t"
+            "subc.cc.u32 %2, %2, %6;\n\t"
+            "subc.u32 %3, %3, %7;"
+            : "+r"(w0), "+r"(w1), "+r"(w2), "+r"(w3)
+            : "r"(t0), "r"(t1), "r"(t2), "r"(t3));
+    }
+    __device__ __forceinline__ void add(float x) {
+        const uint32_t b = __float_as_uint(x);
+        const uint32_t e = (b >> 23) & 0xFFu;
+        const uint32_t m = (b & 0x7FFFFFu) | (e ? 0x800000u : 0u);
+        // value = m * 2^(max(e,1) - 150); as an integer of the format, m << s
+        const int s = (int)(e ? e : 1u) - 150 + FRAC;
+        uint32_t t0 = 0u, t1 = 0u, t2 = 0u, t3 = 0u;
+        if (s < 0) {
+            t0 = s > -32 ? m >> (-s) : 0u;
+        } else {
+            const int wi = s >> 5, bi = s & 31;
+            const uint32_t lo = m << bi, hi = bi ? m >> (32 - bi) : 0u;
+            t0 = wi == 0 ? lo : 0u;
+            t1 = wi == 1 ? lo : (wi == 0 ? hi : 0u);
+            t2 = wi == 2 ? lo : (wi == 1 ? hi : 0u);
+            t3 = wi == 3 ? lo : (wi == 2 ? hi : 0u);
+        }
+        if (b >> 31)
+            sub_words(t0, t1, t2, t3);
+        else
+            add_words(t0, t1, t2, t3);
+    }
+    __device__ __forceinline__ void merge(const Exact128& o) { add_words(o.w0, o.w1, o.w2, o.w3); }
+    // Sum over the warp (every lane gets it).
+    __device__ __forceinline__ void warp_merge() {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            Exact128 p;
+            p.w0 = __shfl_xor_sync(0xffffffffu, w0, o);
+            p.w1 = __shfl_xor_sync(0xffffffffu, w1, o);
+            p.w2 = __shfl_xor_sync(0xffffffffu, w2, o);
+            p.w3 = __shfl_xor_sync(0xffffffffu, w3, o);
+            merge(p);
+        }
+    }
+    // The value, rounded to FP64 (a fixed function of the bits).
+    __device__ double value() const {
+        const bool neg = (w3 >> 31) != 0u;
+        uint32_t a0 = w0, a1 = w1, a2 = w2, a3 = w3;
+        if (neg) {  // magnitude of the two's complement
+            a0 = ~a0, a1 = ~a1, a2 = ~a2, a3 = ~a3;
+            uint64_t c = (uint64_t)a0 + 1u;
+            a0 = (uint32_t)c;
+            c = (uint64_t)a1 + (c >> 32);
+            a1 = (uint32_t)c;
+            c = (uint64_t)a2 + (c >> 32);
+            a2 = (uint32_t)c;
+            a3 = a3 + (uint32_t)(c >> 32);
+        }
+        const double hi = (double)(((uint64_t)a3 << 32) | a2);
+        const double lo = (double)(((uint64_t)a1 << 32) | a0);
+        const double v = (hi * 18446744073709551616.0 + lo) * ldexp(1.0, -FRAC);
+        return neg ? -v : v;
+    }
+};
+
+// Exact fixed-point formats of the sweeps' reductions: PageRank and adjoint
+// terms (changes of ranks, dangling mass) are far below 2^31, resolved to
+// 2^-96; eigenvector norms (squares of row sums, up to the square of the
+// largest weighted in-degree) are resolved to 2^-64 below 2^63.
+using ExactPR = Exact128<96>;
+using ExactEV = Exact128<64>;
+
+// Where a kernel's two exact sums go: one pair of partials per CTA, summed by
+// the last CTA to finish into *out_a, *out_b (FP64).
+struct ExactFold {
+    uint4* part;       // 2 x gridDim.x
+    unsigned* ticket;  // zero before the launch; the last CTA resets it
+    double* out_a;
+    double* out_b;
+    // Optional device-side stop of a power iteration (out_a is the sweep's
+    // L1 change): the last CTA counts the sweep in *iters and sets *stop once
+    // the change is not >= eps (the reference's `while delta >= epsilon`) or
+    // *iters reaches max_iter (0 = no cap).  Kernels of later sweeps read
+    // *stop and return at once.
+    unsigned* stop = nullptr;
+    unsigned long long* iters = nullptr;
+    double eps = 0.0;
+    unsigned long long max_iter = 0;
+};
+
+// Capacity of the per-CTA partials of an ExactFold (every grid is capped to it).
+constexpr unsigned FOLD_MAX_CTAS = 4096;
+
+// CTA of NT threads, every thread passing its (a, b): the CTA's sums go to
+// part[2 * blockIdx.x + {0, 1}], and the last CTA adds all of them.  The
+// totals are exact, so they do not depend on the grid or on which thread
+// summed which terms.
+template <int NT, class E>
+__device__ __forceinline__ void block_fold_exact(E a, E b, const ExactFold& f) {
+    __shared__ uint4 fa[NT / 32], fb[NT / 32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    a.warp_merge();
+    b.warp_merge();
+    if (lane == 0) {
+        fa[warp] = make_uint4(a.w0, a.w1, a.w2, a.w3);
+        fb[warp] = make_uint4(b.w0, b.w1, b.w2, b.w3);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        E ta, tb;
+        for (int w = 0; w < NT / 32; ++w) {
+            ta.add_words(fa[w].x, fa[w].y, fa[w].z, fa[w].w);
+            tb.add_words(fb[w].x, fb[w].y, fb[w].z, fb[w].w);
+        }
+        f.part[2 * blockIdx.x] = make_uint4(ta.w0, ta.w1, ta.w2, ta.w3);
+        f.part[2 * blockIdx.x + 1] = make_uint4(tb.w0, tb.w1, tb.w2, tb.w3);
+        __threadfence();
+        last = atomicAdd(f.ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && warp == 0) {
+        __threadfence();
+        E ta, tb;
+        for (unsigned i = lane; i < gridDim.x; i += 32) {
+            const uint4 pa = __ldcg(f.part + 2 * i), pb = __ldcg(f.part + 2 * i + 1);
+            ta.add_words(pa.x, pa.y, pa.z, pa.w);
+            tb.add_words(pb.x, pb.y, pb.z, pb.w);
+        }
+        ta.warp_merge();
+        tb.warp_merge();
+        if (lane == 0) {
+            const double a = ta.value();
+            *f.out_a = a;
+            *f.out_b = tb.value();
+            *f.ticket = 0u;
+            if (f.stop) {
+                const unsigned long long it = *f.iters + 1;
+                *f.iters = it;
+                if (!(a >= f.eps) || (f.max_iter && it == f.max_iter)) *f.stop = 1u;
+            }
+        }
     }
 }
 

@@ -215,9 +215,7 @@ void build_units(const uint32_t* d_off, const uint32_t* d_other, const uint32_t*
     u.longs.alloc(longs.size(), s);
     u.partial.alloc(slot, s);
     u.counter.alloc(longs.size(), s);
-    u.long_out.alloc(longs.size(), s);
-    const size_t n_buckets = (units.size() + SP_BUCKET - 1) / SP_BUCKET;
-    u.item_out.alloc(n_buckets, s);
+    u.fold_part.alloc(2 * (size_t)FOLD_MAX_CTAS, s);
     if (!units.empty())
         GTC_CUDA(cudaMemcpyAsync(u.units.get(), units.data(), units.size() * sizeof(uint4),
                                  cudaMemcpyHostToDevice, s));

@@ -17,10 +17,11 @@
 //   long rows  SP_CAP-entry chunks, one CTA each; the last CTA of a row
 //       (atomic ticket) folds the chunk partials in chunk order.
 //
-// Every row sum is compensated (Kahan).  A persistent grid walks the work
-// list with a fixed stride, so a row's sum, and the per-CTA partials folded
-// in CTA order at the end, do not depend on timing: the FP32 path is
-// deterministic run to run.
+// Every row sum is compensated (Kahan) in the row's storage order, and the
+// per-row reduction terms (L1 change, dangling mass, squared norm) are
+// summed exactly in 128-bit fixed point, so neither depends on the grid, on
+// timing or on the kernel variant: the FP32 path is deterministic run to
+// run and across variants.
 #pragma once
 
 #include "gtc_internal.cuh"
@@ -33,7 +34,6 @@ constexpr int SP_CAP = 2048;        // entries per long-row chunk; longest mediu
 // SP_HOT entries are the most gathered ones (the rest is read through
 // L1/L2).  One 1024-thread CTA per SM holds them.
 constexpr int SP_HOT = 32768;
-constexpr int SP_FOLD = 256;        // fixed fan-in of the final reduction
 constexpr int SP_BUCKET = 8;        // work items a warp takes together (one fold term)
 constexpr int SP_SLICE_MAX = 128;   // longest row kept in a slice
 constexpr int SP_WINDOW = 2048;     // rows sorted by length inside windows of this many
@@ -65,10 +65,8 @@ struct SweepArgs {
     const float* __restrict__ sw;             // sliced entries: weight (null = Unity)
     float2* partial;
     unsigned* counter;
-    double2* long_out;
     uint32_t n_units, n_long;
     uint32_t hot_n;     // entries of x staged in shared memory (HOT variant)
-    double2* item_out;  // per bucket of SP_BUCKET items: its rows' reduction terms
     // pull half (medium and long rows)
     const uint32_t* __restrict__ off;
     const uint32_t* __restrict__ other;
@@ -86,9 +84,19 @@ struct SweepArgs {
     float uniform, one_minus_d, d;
     const double* psink;                // PageRank: dangling mass of prev
     float alpha, tau;                   // adjoint: shift of the iterate, p . (shifted iterate)
-    // reduction: every item's terms, folded by the last CTA
-    unsigned* ticket;
-    double* out;  // [a, b]
+    // reduction: the rows' (a, b) terms, summed exactly
+    ExactFold fold;
+    const unsigned* stop;  // non-null and set: the iteration has stopped, return at once
+};
+
+// The exact format of a mode's reduction terms.
+template <int MODE>
+struct SweepAcc {
+    using type = ExactPR;
+};
+template <>
+struct SweepAcc<MODE_EIGEN> {
+    using type = ExactEV;
 };
 
 // Classic Kahan accumulator for the inner loops (value = s - c), 4 flops a
@@ -188,22 +196,13 @@ __device__ __forceinline__ float gather(const SweepArgs& A, const float* hot, ui
     return (HOT && s < A.hot_n) ? hot[s] : __ldg(A.x + s);
 }
 
-// Warp sum of a (ta, tb) pair in a fixed shuffle order, as TwoSum pairs.
-__device__ __forceinline__ double2 warp_pair(float ta, float tb) {
-    Kahan ka, kb;
-    ka.s = ta, kb.s = tb;
-    warp_merge_kahan(ka);
-    warp_merge_kahan(kb);
-    return make_double2((double)ka.s + (double)ka.c, (double)kb.s + (double)kb.c);
-}
-
 // NT threads per CTA; HOT: stage x[0 .. hot_n) in shared memory.
 template <int MODE, bool WEIGHTED, int NT, bool HOT>
 __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
     constexpr int SP_WARPS = NT / 32;
     extern __shared__ float hot[];  // x[0 .. hot_n)
-    __shared__ double fa[SP_FOLD], fb[SP_FOLD];
-    __shared__ bool flag;
+    using Acc = typename SweepAcc<MODE>::type;
+    if (A.stop && *A.stop) return;  // the same for every CTA: before any barrier
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float psink = MODE != MODE_EIGEN ? (float)*A.psink : 0.f;
     if (HOT) {
@@ -218,12 +217,12 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
     const uint32_t gw = blockIdx.x * SP_WARPS + warp, nw = gridDim.x * SP_WARPS;
     // A warp takes buckets of up to SP_BUCKET items, bucket b being items
     // b, b + B, b + 2B, ... (B buckets): every bucket mixes heavy and light
-    // items.  The terms of a bucket's rows go to item_out[b] (long rows:
-    // long_out[k]) and the last CTA folds them with a fixed fan-in, so neither
-    // the grid nor the CTA size changes a single bit of the result.
+    // items.  Every row's (a, b) terms are added exactly (Acc), so neither
+    // the grid, the CTA size nor the assignment of items to warps changes a
+    // single bit of the sums.
+    Acc acc_a, acc_b;
     const uint32_t n_buckets = (A.n_units + SP_BUCKET - 1) / SP_BUCKET;
     for (uint32_t bk = gw; bk < n_buckets; bk += nw) {
-    KahanLite bucket_a, bucket_b;
     // the next item's descriptor is loaded while this item runs
     // (the work list and the slices' row lists are read once a sweep:
     // evict-first, like the index stream, so the gathered vector keeps L2)
@@ -295,8 +294,8 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
             if (row != NO_ROW) {
                 float ta, tb;
                 row_finish<MODE>(A, row, rin, acc.value(), psink, ta, tb);
-                bucket_a.add(ta);
-                bucket_b.add(tb);
+                acc_a.add(ta);
+                acc_b.add(tb);
             }
         } else {
             // a medium row, or one chunk of a long row: lanes stride entries
@@ -354,8 +353,8 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
                 if (lane == 0) {
                     float ta, tb;
                     row_finish<MODE>(A, row, rin, k.value(), psink, ta, tb);
-                    bucket_a.add(ta);
-                    bucket_b.add(tb);
+                    acc_a.add(ta);
+                    acc_b.add(tb);
                 }
             } else {
                 // long row: the last warp to finish a chunk folds the chunks
@@ -375,66 +374,19 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
                         A.counter[U.y] = 0u;
                         float ta, tb;
                         sweep_row<MODE>(A, row, t.value(), psink, ta, tb);
-                        // folded by row index, not by whichever warp finished
-                        A.long_out[U.y] = make_double2((double)ta, (double)tb);
+                        acc_a.add(ta);
+                        acc_b.add(tb);
                     }
                 }
             }
         }
     }
 
-        const double2 it = warp_pair(bucket_a.value(), bucket_b.value());
-        if (lane == 0) A.item_out[bk] = it;
     }
 
-    // ---- the last CTA folds every bucket's terms, then the long rows' ----
+    // ---- the CTA's exact sums, added up by the last CTA ----
     __syncthreads();
-    if (tid == 0) {
-        __threadfence();
-        const unsigned t = atomicAdd(A.ticket, 1u);
-        flag = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (flag) {
-        __threadfence();
-        if (tid < SP_FOLD) {
-            // thread t folds a contiguous range, eight loads in flight
-            double ta = 0.0, tb = 0.0;
-            auto fold_range = [&](const double2* v, uint32_t cnt) {
-                const uint32_t per = (cnt + SP_FOLD - 1) / SP_FOLD;
-                const uint32_t b = min(tid * per, cnt), e = min(b + per, cnt);
-                uint32_t i = b;
-                for (; i + 8 <= e; i += 8) {
-                    double2 q[8];
-#pragma unroll
-                    for (int t = 0; t < 8; ++t) q[t] = __ldcg(v + i + t);
-#pragma unroll
-                    for (int t = 0; t < 8; ++t) ta += q[t].x, tb += q[t].y;
-                }
-                for (; i < e; ++i) {
-                    const double2 q = __ldcg(v + i);
-                    ta += q.x, tb += q.y;
-                }
-            };
-            fold_range(A.item_out, n_buckets);
-            fold_range(A.long_out, A.n_long);
-            fa[tid] = ta;
-            fb[tid] = tb;
-        }
-        __syncthreads();
-        for (int w = SP_FOLD / 2; w > 0; w >>= 1) {
-            if (tid < w) {
-                fa[tid] += fa[tid + w];
-                fb[tid] += fb[tid + w];
-            }
-            __syncthreads();
-        }
-        if (tid == 0) {
-            A.out[0] = fa[0];
-            A.out[1] = fb[0];
-            *A.ticket = 0u;
-        }
-    }
+    block_fold_exact<NT>(acc_a, acc_b, A.fold);
 }
 
 }  // namespace gtc

@@ -99,7 +99,7 @@ void View::prepare(gtc_graph* g, const gtc_view* v, cudaStream_t s, uint64_t* L)
         pull_eid = pull_src.eid.get();
         push_off = push_src.off.get(), push_other = push_src.other.get(),
         push_eid = push_src.eid.get();
-        m_pull = g->m;
+        m_pull = g->m_live;
         return;
     }
     DevBuf<uint8_t> dv, de;
@@ -122,9 +122,9 @@ void View::prepare(gtc_graph* g, const gtc_view* v, cudaStream_t s, uint64_t* L)
         GTC_CUDA(cudaMemcpyAsync(de.get(), he, g->m, cudaMemcpyHostToDevice, s));
     }
     const uint8_t* vnew = hv ? active.get() : nullptr;  // the mask in internal labels
-    compact_half(n, g->m, pull_src.off.get(), pull_src.other.get(), pull_src.eid.get(), vnew,
+    compact_half(n, g->m_live, pull_src.off.get(), pull_src.other.get(), pull_src.eid.get(), vnew,
                  de.get(), fpull, s, L);
-    compact_half(n, g->m, push_src.off.get(), push_src.other.get(), push_src.eid.get(), vnew,
+    compact_half(n, g->m_live, push_src.off.get(), push_src.other.get(), push_src.eid.get(), vnew,
                  de.get(), fpush, s, L);
     GTC_CUDA(cudaStreamSynchronize(s));
     pull_off = fpull.off.get(), pull_other = fpull.other.get(), pull_eid = fpull.eid.get();

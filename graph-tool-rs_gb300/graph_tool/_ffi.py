@@ -95,6 +95,8 @@ SIGNATURES = {
     "gtc_graph_create": (C.c_int, [C.c_uint64, C.c_uint64, u32p, u32p, C.POINTER(C.c_void_p)]),
     "gtc_graph_create_device": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.POINTER(C.c_void_p)]),
+    "gtc_graph_create_blocks": (C.c_int, [C.c_uint64, C.c_uint64, u64p, u32p, u32p,
+                                          C.POINTER(C.c_void_p)]),
     "gtc_graph_destroy": (C.c_int, [C.c_void_p]),
     "gtc_graph_info": (C.c_int, [C.c_void_p, u64p, u64p, u64p]),
     "gtc_graph_export": (C.c_int, [C.c_void_p, u64p, u32p, u32p, u64p, u32p, u32p]),

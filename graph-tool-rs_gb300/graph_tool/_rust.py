@@ -113,6 +113,32 @@ class Graph:
         self.directed = True
 
     @classmethod
+    def from_blocks(cls, n: int, edge_bound: int, block_off, out_len, entries) -> "Graph":
+        """A graph from the reference's adjacency blocks as stored
+        (gtc_graph_create_blocks): vertex v's Block is entries[block_off[v] ..
+        block_off[v+1]) of (other, idx) pairs, out-half first (out_len[v]
+        entries).  Edge ids below ``edge_bound`` that no entry uses are
+        removed edges; edge maps are indexed up to ``edge_bound``.  The graph
+        is read-only here (its history of removals has no edge-list form)."""
+        block_off = np.ascontiguousarray(block_off, dtype=np.uint64)
+        out_len = np.ascontiguousarray(out_len, dtype=np.uint32)
+        entries = np.ascontiguousarray(entries, dtype=np.uint32).reshape(-1)
+        if block_off.size != n + 1 or out_len.size != n:
+            raise ValueError("block_off needs n + 1 entries and out_len n")
+        if entries.size != 2 * int(block_off[-1] if n else 0):
+            raise ValueError("entries must hold 2 uint32 per block entry")
+        h = C.c_void_p()
+        _ffi.check(_ffi.lib().gtc_graph_create_blocks(
+            int(n), int(edge_bound), _ffi.ptr(block_off, _ffi.u64p), _ffi.ptr(out_len, _ffi.u32p),
+            _ffi.ptr(entries, _ffi.u32p), C.byref(h)))
+        nv, eb, live = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _ffi.check(_ffi.lib().gtc_graph_info(h, C.byref(nv), C.byref(eb), C.byref(live)))
+        g = cls._from_handle(h.value, nv.value, live.value)
+        g._bound = int(eb.value)
+        g._frozen = True
+        return g
+
+    @classmethod
     def _from_handle(cls, handle, n: int, m: int) -> "Graph":
         """Adopt a gtc_graph built elsewhere (the .gt reader); its edge list
         is copied back from the device only when asked for."""
@@ -128,10 +154,12 @@ class Graph:
         return self._m
 
     def edge_index_range(self) -> int:
-        return self._m
+        return getattr(self, "_bound", self._m)
 
     # ---- mutation -----------------------------------------------------
     def _dirty(self):
+        if getattr(self, "_frozen", False):
+            raise RuntimeError("a graph built from blocks is read-only")
         if self._lazy:
             self.edges()  # the handle is the only copy of the edges so far
         self._flat = None

@@ -175,10 +175,30 @@ int gtc_graph_create(uint64_t n, uint64_t m, const uint32_t* src, const uint32_t
 int gtc_graph_create_device(uint64_t n, uint64_t m, const uint32_t* d_src,
                             const uint32_t* d_tgt, void* stream, gtc_graph** out);
 
+/* Build a graph from the reference's adjacency blocks as they are stored,
+ * whatever history made them (add_edge, remove_edge with its swap-remove,
+ * crates/gt-core/src/adj/block.rs:241-291, edge ids reused from the LIFO free
+ * list, crates/gt-core/src/adj/alloc.rs:58-90): the drop-in for a caller
+ * holding an AdjList (crates/gt-core/src/adj/list.rs:26-40).  Vertex v's
+ * Block (block.rs:54-57) is entries[block_off[v] .. block_off[v+1]), its
+ * out-half the first out_len[v] of them and its in-half the rest; an entry
+ * is the 8-byte AdjEntry {other, idx} (crates/gt-core/src/adj/entry.rs:39-48)
+ * as two uint32, so a concatenation of every Block::all() can be passed as
+ * is.  edge_bound is AdjList::edge_bound (list.rs:130); ids below it that no
+ * entry uses are removed edges, and weight maps stay indexed by EdgeId up to
+ * it.  Every live edge must appear once in its source's out-half and once in
+ * its target's in-half (else GTC_ERR_ARG; an index out of range is
+ * GTC_ERR_INDEX).  The pull visits every in-half in the given order, so the
+ * FP64-exact solves are bit-identical to the reference's on this graph.
+ * Host arrays. */
+int gtc_graph_create_blocks(uint64_t n, uint64_t edge_bound, const uint64_t* block_off,
+                            const uint32_t* out_len, const uint32_t* entries, gtc_graph** out);
+
 int gtc_graph_destroy(gtc_graph* g);
 
 /* Vertex bound, edge bound (AdjList::vertex_bound / edge_bound,
- * crates/gt-core/src/graph.rs:63-67) and live edge count. */
+ * crates/gt-core/src/graph.rs:63-67) and live edge count (below the edge
+ * bound when ids have holes, gtc_graph_create_blocks). */
 int gtc_graph_info(const gtc_graph* g, uint64_t* n, uint64_t* edge_bound, uint64_t* num_edges);
 
 /* Copy the blocks back to host memory: for every vertex its out-half

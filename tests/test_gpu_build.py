@@ -80,3 +80,40 @@ def test_bad_vertex_is_a_value_error(gtc):
     st = _ffi.lib().gtc_graph_create(3, 2, _ffi.ptr(src, _ffi.u32p), _ffi.ptr(tgt, _ffi.u32p),
                                      C.byref(h))
     assert st == _ffi.GTC_ERR_ARG and b"no such vertex" in _ffi.lib().gtc_last_error()
+
+
+def test_first_handle_of_a_fresh_process_keeps_its_sizes(gtc):
+    """The first gtc_graph of a process, built before anything else touched
+    the GPU, reports the sizes it was built with and solves over all its
+    edges (a solve over an edgeless graph would return the uniform vector)."""
+    import subprocess
+    import sys
+    code = r'''
+import ctypes as C, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from graph_tool import _ffi
+L = _ffi.lib()
+n, m = 6, 7
+src = np.array([0, 1, 2, 3, 4, 5, 0], np.uint32)
+tgt = np.array([1, 2, 0, 4, 5, 3, 3], np.uint32)
+h = C.c_void_p()
+_ffi.check(L.gtc_graph_create(n, m, _ffi.ptr(src, _ffi.u32p), _ffi.ptr(tgt, _ffi.u32p), C.byref(h)))
+a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+_ffi.check(L.gtc_graph_info(h, C.byref(a), C.byref(b), C.byref(c)))
+assert (a.value, b.value, c.value) == (n, m, m), (a.value, b.value, c.value)
+r = np.full(n, 1.0 / n)
+p = _ffi.PowerIteration(1e-10, 200, n, 1)
+res = _ffi.Result()
+_ffi.check(L.gtc_pagerank(h, None, None, 0, None, 0, 0.85, C.byref(p), _ffi.ptr(r, _ffi.f64p), n,
+                          n, None, C.byref(res)))
+assert abs(r.sum() - 1.0) < 1e-5 and r.max() - r.min() > 1e-3, r
+print("ok", res.iterations)
+'''
+    import os
+    pkg = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                       "graph-tool-rs_gb300")
+    out = subprocess.run([sys.executable, "-c", code, pkg], capture_output=True, text=True,
+                         timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.startswith("ok")

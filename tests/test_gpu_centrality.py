@@ -189,5 +189,5 @@ def test_f32_eigenvector_rel_l1(oracle, gtc, er10k):
                                                       epsilon=1e-7, max_iter=500)
     err = _rel_l1(got, want)
     print(f"eigen f32: rel L1 {err:.3e}, eig {eg} vs {ew}, sweeps {ig} vs {iw}")
-    assert err < 1e-5
+    assert err < 1e-6
     assert abs(eg - ew) / ew < 1e-6

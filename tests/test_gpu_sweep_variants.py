@@ -117,11 +117,15 @@ def test_pagerank_every_schedule(oracle, gtc, tiers, kind):
 def test_eigenvector_every_schedule(oracle, gtc, tiers, kind):
     n, src, tgt = tiers
     kw = _kwargs(kind, n, src.size, np.random.default_rng(8))
-    want, ew, iw = K.OracleSolver(oracle).eigenvector(n, src, tgt, grain=4096, epsilon=1e-6,
+    # epsilon 1e-5: above the FP32 floor of the L1 change of a normalised
+    # vector of 50,000 entries (near 1e-6 the FP32 iterate's rounding noise
+    # delays the stop by a few sweeps while the vector is already within
+    # 1e-7 of the oracle's)
+    want, ew, iw = K.OracleSolver(oracle).eigenvector(n, src, tgt, grain=4096, epsilon=1e-5,
                                                       max_iter=1000, **kw)
     first = None
     for sched in SCHEDULES:
-        got, ig, eg = _gpu(gtc, n, src, tgt, sched, "eigenvector", 1e-6, **dict(kw))
+        got, ig, eg = _gpu(gtc, n, src, tgt, sched, "eigenvector", 1e-5, **dict(kw))
         err = _rel_l1(got, want)
         print(f"eigenvector {kind} {sched}: rel L1 {err:.3e}, eigenvalue {eg!r} vs {ew!r}, "
               f"sweeps {ig} vs {iw}")
