@@ -697,12 +697,117 @@ DevBuf<float> sliced_weights(const Units& u, const SolveIn& in, cudaStream_t s, 
     return sw;
 }
 
+// A 64-bit hash of a weight map's bits: the sum over entries of a mixed
+// (bits, index) word (the SplitMix64 finaliser), so any change of any entry
+// changes it with overwhelming probability, and the sum does not depend on
+// the grid.
+__global__ void k_weight_hash(uint64_t m, const void* __restrict__ w, int wdt,
+                              unsigned long long* __restrict__ out) {
+    unsigned long long h = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long bits = wdt == GTC_F64 ? ((const unsigned long long*)w)[i]
+                                                       : ((const uint32_t*)w)[i];
+        unsigned long long z = bits + (i + 1) * 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        h += z ^ (z >> 31);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, h);
+}
+
+// The handle's weight layouts for weight map w (FP32 path, unfiltered
+// views): the cache is kept when w is the map it was built from, cleared
+// otherwise.
+WeightCache& weight_cache(gtc_graph* g, const DVec& w, cudaStream_t s, uint64_t* L) {
+    WeightCache& c = g->wcache;
+    DevBuf<unsigned long long> dh(1, s);
+    GTC_CUDA(cudaMemsetAsync(dh.get(), 0, sizeof(unsigned long long), s));
+    if (g->m) {
+        k_weight_hash<<<(unsigned)sm_count() * 8, 256, 0, s>>>(g->m, w.p, w.dtype, dh.get());
+        GTC_LAUNCHED();
+        (*L)++;
+    }
+    unsigned long long h = 0;
+    GTC_CUDA(cudaMemcpyAsync(&h, dh.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
+    GTC_CUDA(cudaStreamSynchronize(s));
+    if (!(c.valid && c.ptr == w.p && c.dtype == w.dtype && c.hash == h)) {
+        GTC_CUDA(cudaStreamSynchronize(g->home));  // buffers of the old map are free to go
+        c.reset();
+        c.ptr = w.p, c.dtype = w.dtype, c.hash = h, c.valid = true;
+    }
+    return c;
+}
+
+// FP32 weights in the storage order of the in-halves (h = 0) or the
+// out-halves (h = 1).
+const float* cached_half_weights(gtc_graph* g, WeightCache& c, int h, cudaStream_t s,
+                                 uint64_t* L) {
+    const uint32_t m = g->m_live;
+    if (!c.half[h].get()) {
+        c.half[h].alloc(m, g->home);
+        GTC_CUDA(cudaStreamSynchronize(s));
+        if (m) {
+            const Halves& hv = h ? g->out : g->in;
+            k_gather_w<float><<<grid_for(m, 256, 1u << 30), 256, 0, g->home>>>(
+                m, hv.eid.get(), c.ptr, c.dtype, c.half[h].get());
+            GTC_LAUNCHED();
+            (*L)++;
+        }
+        GTC_CUDA(cudaStreamSynchronize(g->home));
+    }
+    return c.half[h].get();
+}
+
+// Weighted degree (FP32 compensated sums, FP64 result) over the out-halves
+// (h = 1, the plain view's push half) or the in-halves (h = 0).
+void cached_degrees(gtc_graph* g, WeightCache& c, int h, cudaStream_t s, uint64_t* L,
+                    const double** deg, const uint8_t** sink) {
+    const uint32_t n = g->n;
+    if (!c.deg[h].get()) {
+        const float* wh = cached_half_weights(g, c, h, s, L);
+        c.deg[h].alloc(n, g->home);
+        c.sink[h].alloc(n, g->home);
+        if (n) {
+            k_degree_f32<<<grid_for((size_t)n * 8, 256, 1u << 30), 256, 0, g->home>>>(
+                n, (h ? g->out : g->in).off.get(), wh, nullptr, c.deg[h].get(), c.sink[h].get());
+            GTC_LAUNCHED();
+            (*L)++;
+        }
+        GTC_CUDA(cudaStreamSynchronize(g->home));
+    }
+    *deg = c.deg[h].get();
+    *sink = c.sink[h].get();
+}
+
+// The sliced entries' weights of a cached pull schedule (k = 0: units_in,
+// k = 1: units_out).
+const float* cached_sliced_weights(gtc_graph* g, WeightCache& c, int k, const Units& u,
+                                   cudaStream_t s, uint64_t* L) {
+    if (!u.n_sliced) return nullptr;
+    if (!c.sliced[k].get()) {
+        c.sliced[k].alloc(u.n_sliced, g->home);
+        GTC_CUDA(cudaStreamSynchronize(s));
+        k_gather_sw<<<grid_for(u.n_sliced, 256, 1u << 30), 256, 0, g->home>>>(
+            u.n_sliced, u.seid.get(), c.ptr, c.dtype, c.sliced[k].get());
+        GTC_LAUNCHED();
+        (*L)++;
+        GTC_CUDA(cudaStreamSynchronize(g->home));
+    }
+    return c.sliced[k].get();
+}
+
 // Everything a sweep loop needs that does not change between sweeps.
 struct Prep {
     View view;
     double uniform = 0.0;
     DevBuf<double> deg;
     DevBuf<uint8_t> sink;
+    const double* degp = nullptr;   // deg, or the handle's cached weighted degrees
+    const uint8_t* sinkp = nullptr;
+    WeightCache* wc = nullptr;      // the handle's weight layouts (FP32, unfiltered, weighted)
     DevBuf<double> x64;  // initial iterate, FP64
 };
 
@@ -712,9 +817,15 @@ void prepare(gtc_graph* g, const gtc_view* vw, const SolveIn& in, bool need_deg,
     P.view.prepare(g, vw, s, L);
     const uint32_t n = P.view.n;
     P.uniform = P.view.n_active == 0 ? 0.0 : 1.0 / (double)P.view.n_active;
-    if (need_deg) {
+    if (in.weight.present() && in.precision == GTC_PREC_F32 && !P.view.filtered)
+        P.wc = &weight_cache(g, in.weight, s, L);
+    if (need_deg && P.wc) {
+        cached_degrees(g, *P.wc, P.view.reversed ? 0 : 1, s, L, &P.degp, &P.sinkp);
+    } else if (need_deg) {
         P.deg.alloc(n, s);
         P.sink.alloc(n, s);
+        P.degp = P.deg.get();
+        P.sinkp = P.sink.get();
         if (n && in.weight.present() && in.precision == GTC_PREC_F32) {
             const uint32_t mp = P.view.m_pull;  // the push half holds as many entries
             DevBuf<float> wout(mp, s);
@@ -755,6 +866,14 @@ void store_result(gtc_graph* g, uint32_t n, const T* src, const Prep& P, const S
     (*L)++;
 }
 
+// The FP32 weights a sweep streams: the handle's cached layouts for an
+// unfiltered view, else gathered for this call into `own`.
+struct SweepWeights {
+    DevBuf<float> own_pull, own_sliced;
+    const float* pull = nullptr;
+    const float* sliced = nullptr;
+};
+
 template <class T>
 DevBuf<T> pull_weights(const Prep& P, const SolveIn& in, cudaStream_t s, uint64_t* L) {
     DevBuf<T> w;
@@ -767,6 +886,19 @@ DevBuf<T> pull_weights(const Prep& P, const SolveIn& in, cudaStream_t s, uint64_
         (*L)++;
     }
     return w;
+}
+
+void sweep_weights(gtc_graph* g, const Prep& P, const SolveIn& in, const Units& U, bool rev,
+                   cudaStream_t s, uint64_t* L, SweepWeights& out) {
+    if (P.wc) {
+        out.pull = cached_half_weights(g, *P.wc, rev ? 1 : 0, s, L);
+        out.sliced = cached_sliced_weights(g, *P.wc, rev ? 1 : 0, U, s, L);
+        return;
+    }
+    out.own_pull = pull_weights<float>(P, in, s, L);
+    out.own_sliced = sliced_weights(U, in, s, L);
+    out.pull = out.own_pull.get();
+    out.sliced = out.own_sliced.get();
 }
 
 }  // namespace
@@ -792,7 +924,7 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         // sinks in vertex order and their Plan (grain_of, centrality.rs:186-188, :311)
         DevBuf<uint32_t> flag32(n, s), pos((size_t)n + 1, s);
         if (n) {
-            k_sink_flags<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->iperm.get(), P.sink.get(),
+            k_sink_flags<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->iperm.get(), P.sinkp,
                                                                   flag32.get());
             GTC_LAUNCHED();
             L++;
@@ -836,10 +968,10 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
             k_fold<<<1, 32, 0, s>>>(sink_chunks, part.get(), scal.get(), nullptr, 0);
             if (n) {
                 k_pr_f64_rows<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(
-                    n, view.pull_off, view.pull_other, wpull.get(), P.deg.get(), act, pers64,
+                    n, view.pull_off, view.pull_other, wpull.get(), P.degp, act, pers64,
                     P.uniform, 1.0 - d, d, scal.get(), cur, nxt, diff.get());
                 k_pr_f64_long<<<(unsigned)sm_count() * 8, 256, 0, s>>>(
-                    n, view.pull_off, view.pull_other, wpull.get(), P.deg.get(), act, pers64,
+                    n, view.pull_off, view.pull_other, wpull.get(), P.degp, act, pers64,
                     P.uniform, 1.0 - d, d, scal.get(), cur, nxt, diff.get());
             }
             // the delta is folded over the Plan in original vertex order
@@ -863,11 +995,10 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
     } else {
         DevBuf<float> invdeg(n, s);
         if (n) {
-            k_invdeg_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.deg.get(), invdeg.get());
+            k_invdeg_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.degp, invdeg.get());
             GTC_LAUNCHED();
             L++;
         }
-        DevBuf<float> wpull = pull_weights<float>(P, in, s, &L);
         DevBuf<float> pers32;
         if (in.pers.present() && n) {
             pers32.alloc(n, s);
@@ -892,7 +1023,7 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         const unsigned nb = persistent_blocks(n);
         FoldBufs fb(nb, s);
         double* dp = fb.out.get();  // [0] delta, [1] dangling mass of the current iterate
-        k_pr_prime<<<nb, PR_NT, 0, s>>>(n, r0.get(), invdeg.get(), P.sink.get(), y0.get(),
+        k_pr_prime<<<nb, PR_NT, 0, s>>>(n, r0.get(), invdeg.get(), P.sinkp, y0.get(),
                                        fb.fold(dp + 2, dp + 1));
         GTC_LAUNCHED();
         L++;
@@ -906,12 +1037,13 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         GTC_CUDA(cudaMemcpyAsync(dq + 1, dp + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
         SweepArgs A{};
         set_schedule(A, *U, view);
-        DevBuf<float> swt = sliced_weights(*U, in, s, &L);
-        A.sw = swt.get();
-        A.w = wpull.get();
+        SweepWeights sw8;
+        sweep_weights(g, P, in, *U, view.reversed, s, &L, sw8);
+        A.sw = sw8.sliced;
+        A.w = sw8.pull;
         A.active = act;
         A.invdeg = invdeg.get();
-        A.sink = P.sink.get();
+        A.sink = P.sinkp;
         A.pers = pers32.get();
         A.uniform = (float)P.uniform;
         A.one_minus_d = (float)(1.0 - d);
@@ -1021,7 +1153,6 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         res->device_ms = total.ms();
         store_result<double>(g, n, cur, P, in, s, &L);
     } else {
-        DevBuf<float> wpull = pull_weights<float>(P, in, s, &L);
         DevBuf<float> x0((size_t)n + 1, s), x1((size_t)n + 1, s);  // x[n] == 0: slice padding
         GTC_CUDA(cudaMemsetAsync(x0.get() + n, 0, sizeof(float), s));
         GTC_CUDA(cudaMemsetAsync(x1.get() + n, 0, sizeof(float), s));
@@ -1041,9 +1172,10 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         float *xc = x0.get(), *xn = x1.get();
         SweepArgs A{};
         set_schedule(A, *U, view);
-        DevBuf<float> swt = sliced_weights(*U, in, s, &L);
-        A.sw = swt.get();
-        A.w = wpull.get();
+        SweepWeights sw8;
+        sweep_weights(g, P, in, *U, view.reversed, s, &L, sw8);
+        A.sw = sw8.sliced;
+        A.w = sw8.pull;
         A.active = act;
         A.fold = ExactFold{U->fold_part.get(), f1.ticket.get(), o1, o1 + 1};
         A.x = xc, A.prev = xc, A.next = xn;
@@ -1209,27 +1341,37 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     rv.reversed = (vw && vw->reversed) ? 0 : 1;
     View av;
     av.prepare(g, &rv, s, &L);
-    DevBuf<float> wpull;
-    if (W && av.m_pull) {
-        wpull.alloc(av.m_pull, s);
-        k_gather_w<float><<<grid_for(av.m_pull, 256, 1u << 30), 256, 0, s>>>(
-            av.m_pull, av.pull_eid, in.weight.p, in.weight.dtype, wpull.get());
-        GTC_LAUNCHED();
-        L++;
-    }
-    if (W) {
+    // the weights the adjoint streams and the forward's weighted degrees:
+    // from the handle's cache (the forward solve normally built them)
+    const int hav = av.reversed ? 1 : 0;  // the half the adjoint pulls over
+    DevBuf<float> wpull_own;
+    const float* wpull = nullptr;
+    if (W && P.wc) {
+        wpull = cached_half_weights(g, *P.wc, hav, s, &L);
+        cached_degrees(g, *P.wc, hav, s, &L, &P.degp, &P.sinkp);
+    } else if (W) {
+        if (av.m_pull) {
+            wpull_own.alloc(av.m_pull, s);
+            k_gather_w<float><<<grid_for(av.m_pull, 256, 1u << 30), 256, 0, s>>>(
+                av.m_pull, av.pull_eid, in.weight.p, in.weight.dtype, wpull_own.get());
+            GTC_LAUNCHED();
+            L++;
+        }
+        wpull = wpull_own.get();
         P.deg.alloc(n, s);
         P.sink.alloc(n, s);
+        P.degp = P.deg.get();
+        P.sinkp = P.sink.get();
         if (n) {
             k_degree_f32<<<grid_for((size_t)n * 8, TB, 1u << 30), TB, 0, s>>>(
-                n, av.pull_off, wpull.get(), nullptr, P.deg.get(), P.sink.get());
+                n, av.pull_off, wpull, nullptr, P.deg.get(), P.sink.get());
             GTC_LAUNCHED();
             L++;
         }
     }
     DevBuf<float> invdeg(n, s), pers32, g32(n, s), pi32(n, s), ypi((size_t)n + 1, s);
     if (n) {
-        k_invdeg_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.deg.get(), invdeg.get());
+        k_invdeg_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.degp, invdeg.get());
         k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.x64.get(), GTC_F64, nullptr, pi32.get());
         k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, in.gpi.p, in.gpi.dtype, g->perm.get(),
                                                           g32.get());
@@ -1247,7 +1389,7 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     FoldBufs fb(nb, s);
     double* dp = fb.out.get();  // [1] dangling mass of pi
     // y = pi / deg and the dangling mass of pi
-    k_pr_prime<<<nb, PR_NT, 0, s>>>(n, pi32.get(), invdeg.get(), P.sink.get(), ypi.get(),
+    k_pr_prime<<<nb, PR_NT, 0, s>>>(n, pi32.get(), invdeg.get(), P.sinkp, ypi.get(),
                                    fb.fold(dp + 2, dp + 1));
     GTC_LAUNCHED();
     L++;
@@ -1279,11 +1421,18 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     double* dq = fs.out.get();  // [0] residual, [1] p . (next iterate before its shift)
     SweepArgs A{};
     set_schedule(A, *U, av);
-    DevBuf<float> swt = sliced_weights(*U, fin, s, &L);
-    A.sw = swt.get();
-    A.w = wpull.get();
+    DevBuf<float> swt_own;
+    const float* swt = nullptr;
+    if (W && P.wc) {
+        swt = cached_sliced_weights(g, *P.wc, hav, *U, s, &L);
+    } else {
+        swt_own = sliced_weights(*U, fin, s, &L);
+        swt = swt_own.get();
+    }
+    A.sw = swt;
+    A.w = wpull;
     A.invdeg = invdeg.get();
-    A.sink = P.sink.get();
+    A.sink = P.sinkp;
     A.pers = pers32.get();
     A.gvec = g32.get();
     A.uniform = uni;
@@ -1343,7 +1492,7 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
         k_row_ids<<<grid_for((size_t)n * 8, TB, 1u << 30), TB, 0, s>>>(n, av.pull_off, rowid.get());
         k_grad_w<<<grid_for(av.m_pull, TB, 1u << 30), TB, 0, s>>>(
             av.m_pull, rowid.get(), av.pull_other, av.pull_eid, ypi.get(), lc, atl.get(),
-            P.sink.get(), (float)d, (float)(alpha - alpha_prev), in.grad_w, in.grad_w_dtype);
+            P.sinkp, (float)d, (float)(alpha - alpha_prev), in.grad_w, in.grad_w_dtype);
         GTC_LAUNCHED();
         L += 2;
     }

@@ -124,6 +124,29 @@ struct Units {
     bool built = false;
 };
 
+// FP32 edge weights laid out for the sweeps, kept on the handle between
+// solves (gtc_centrality.cu): the caller's weight map by EdgeId is gathered
+// into the storage order of the in-halves and the out-halves, into the
+// sliced entries of each pull schedule, and summed into weighted degrees,
+// once; later solves with the same map reuse them.  The key is the map's
+// address, dtype and a 64-bit hash of its contents (one sequential read per
+// solve), so a map changed in place is gathered again.
+struct WeightCache {
+    const void* ptr = nullptr;
+    int dtype = -1;
+    unsigned long long hash = 0;
+    bool valid = false;
+    DevBuf<float> half[2];      // [0] in-half order, [1] out-half order
+    DevBuf<float> sliced[2];    // sliced entries of units_in [0] / units_out [1]
+    DevBuf<double> deg[2];      // weighted degree over the in-halves [0] / out-halves [1]
+    DevBuf<uint8_t> sink[2];    // zero weighted degree
+    void reset() {
+        for (int h = 0; h < 2; ++h) half[h].release(), sliced[h].release(), deg[h].release(),
+                                    sink[h].release();
+        valid = false;
+    }
+};
+
 // Pull schedule of the batched personalised PageRank (gtc_ppr.cu): rows with
 // more in-edges than one chunk are cut into chunks, the rest are rows of
 // their own, heaviest first.
@@ -221,6 +244,7 @@ struct gtc_graph {
     gtc::Halves out;  // CSR: out-halves (out_edges order)
     gtc::Halves in;   // CSC: in-halves (in_edges order, the pull order)
     gtc::Units units_in, units_out;  // pull schedules of the plain and reversed views
+    gtc::WeightCache wcache;         // FP32 weight layouts of the last weight map used
     gtc::PprSched ppr_sched[2];      // batched schedules of the plain and reversed views
     gtc::DevBuf<float> ppr_z[2];     // batched iterates, kept between calls (grown on demand)
     uint64_t launches = 0;  // kernels this handle has launched (diagnostics)
