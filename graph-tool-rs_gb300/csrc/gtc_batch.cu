@@ -77,6 +77,7 @@ struct GbArgs {
     float one_minus_d, d;
     double epsilon;
     uint64_t max_iter;
+    uint64_t sweep_limit;  // an uncapped solve gives up after this many sweeps
     void* out;
     int out_dtype;
     uint64_t* iters;     // per graph, then a flag word (GB_NONFINITE | GB_SWEEP_CAP)
@@ -89,6 +90,7 @@ struct GbArgs {
 // uncapped solve (max_iter 0) gives up after GB_UNCAPPED sweeps; both set a
 // flag the host turns into an error.
 constexpr uint64_t GB_UNCAPPED = 100000;
+uint64_t g_sweep_limit = GB_UNCAPPED;  // lowered only by gtc_debug_set_batch_sweep_limit
 constexpr uint64_t GB_NONFINITE = 1, GB_SWEEP_CAP = 2;
 
 __device__ __forceinline__ bool sweep_done(const GbArgs& A, double delta, uint64_t it) {
@@ -98,7 +100,7 @@ __device__ __forceinline__ bool sweep_done(const GbArgs& A, double delta, uint64
         if (threadIdx.x == 0) atomicOr((unsigned long long*)(A.iters + A.G_all), GB_NONFINITE);
         return true;
     }
-    if (it == GB_UNCAPPED) {
+    if (it == A.sweep_limit) {
         if (threadIdx.x == 0) atomicOr((unsigned long long*)(A.iters + A.G_all), GB_SWEEP_CAP);
         return true;
     }
@@ -686,7 +688,7 @@ void pagerank_batch(gtc_graph_batch* b, const DVec& weight, double damping, doub
     const bool W = weight.present();
     // the launches of one solve, captured once per set of inputs and replayed
     const BatchKey key{W ? weight.p : nullptr, W ? weight.dtype : -1, out, out_dtype, damping,
-                       epsilon, max_iter};
+                       epsilon, max_iter, g_sweep_limit};
     if (!b->exec || !(b->key == key)) {
         if (b->exec) {
             cudaGraphExecDestroy(b->exec);
@@ -759,6 +761,7 @@ void pagerank_batch(gtc_graph_batch* b, const DVec& weight, double damping, doub
         A.d = (float)damping;
         A.epsilon = epsilon;
         A.max_iter = max_iter;
+        A.sweep_limit = g_sweep_limit;
         A.out = out;
         A.out_dtype = out_dtype;
         A.iters = b->iters.get();
@@ -819,7 +822,13 @@ void pagerank_batch(gtc_graph_batch* b, const DVec& weight, double damping, doub
     GTC_REQUIRE(!(flags & GB_NONFINITE), GTC_ERR_ARG,
                 "a graph's L1 change is not a finite number (non-finite weights?)");
     GTC_REQUIRE(!(flags & GB_SWEEP_CAP), GTC_ERR_TIMEOUT,
-                "an uncapped solve (max_iter 0) did not converge within 100000 sweeps");
+                "an uncapped solve (max_iter 0) did not converge within " +
+                    std::to_string(g_sweep_limit) + " sweeps");
 }
 
 }  // namespace gtc
+
+extern "C" int gtc_debug_set_batch_sweep_limit(uint64_t limit) {
+    gtc::g_sweep_limit = limit ? limit : gtc::GB_UNCAPPED;
+    return GTC_OK;
+}

@@ -704,10 +704,14 @@ DevBuf<float> sliced_weights(const Units& u, const SolveIn& in, cudaStream_t s, 
 __global__ void k_weight_hash(uint64_t m, const void* __restrict__ w, int wdt,
                               unsigned long long* __restrict__ out) {
     unsigned long long h = 0;
+    unsigned bad = 0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const unsigned long long bits = wdt == GTC_F64 ? ((const unsigned long long*)w)[i]
                                                        : ((const uint32_t*)w)[i];
+        // a non-finite weight: all exponent bits set
+        bad |= wdt == GTC_F64 ? ((bits >> 52) & 0x7FFull) == 0x7FFull
+                              : ((bits >> 23) & 0xFFull) == 0xFFull;
         unsigned long long z = bits + (i + 1) * 0x9E3779B97F4A7C15ull;
         z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
         z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
@@ -715,24 +719,39 @@ __global__ void k_weight_hash(uint64_t m, const void* __restrict__ w, int wdt,
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(out, h);
+    bad = __any_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out, h);
+        if (bad) atomicOr(out + 1, 1ull);
+    }
 }
 
-// The handle's weight layouts for weight map w (FP32 path, unfiltered
-// views): the cache is kept when w is the map it was built from, cleared
-// otherwise.
-WeightCache& weight_cache(gtc_graph* g, const DVec& w, cudaStream_t s, uint64_t* L) {
-    WeightCache& c = g->wcache;
-    DevBuf<unsigned long long> dh(1, s);
-    GTC_CUDA(cudaMemsetAsync(dh.get(), 0, sizeof(unsigned long long), s));
-    if (g->m) {
-        k_weight_hash<<<(unsigned)sm_count() * 8, 256, 0, s>>>(g->m, w.p, w.dtype, dh.get());
+}  // namespace
+
+// One read of a weight map by EdgeId (m entries): its 64-bit content hash,
+// and a refusal (GTC_ERR_ARG) if it holds a NaN or an infinity.
+unsigned long long scan_weights(const DVec& w, uint64_t m, cudaStream_t s, uint64_t* L) {
+    DevBuf<unsigned long long> dh(2, s);
+    GTC_CUDA(cudaMemsetAsync(dh.get(), 0, 2 * sizeof(unsigned long long), s));
+    if (m) {
+        k_weight_hash<<<(unsigned)sm_count() * 8, 256, 0, s>>>(m, w.p, w.dtype, dh.get());
         GTC_LAUNCHED();
         (*L)++;
     }
-    unsigned long long h = 0;
-    GTC_CUDA(cudaMemcpyAsync(&h, dh.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
+    unsigned long long h[2] = {0, 0};
+    GTC_CUDA(cudaMemcpyAsync(h, dh.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
     GTC_CUDA(cudaStreamSynchronize(s));
+    GTC_REQUIRE(h[1] == 0, GTC_ERR_ARG, "weight map holds a non-finite value (NaN or infinity)");
+    return h[0];
+}
+
+namespace {
+
+// The handle's weight layouts for weight map w (FP32 path, unfiltered
+// views): the cache is kept when w is the map it was built from (same
+// address, dtype and content hash), cleared otherwise.
+WeightCache& weight_cache(gtc_graph* g, const DVec& w, unsigned long long h) {
+    WeightCache& c = g->wcache;
     if (!(c.valid && c.ptr == w.p && c.dtype == w.dtype && c.hash == h)) {
         GTC_CUDA(cudaStreamSynchronize(g->home));  // buffers of the old map are free to go
         c.reset();
@@ -817,8 +836,10 @@ void prepare(gtc_graph* g, const gtc_view* vw, const SolveIn& in, bool need_deg,
     P.view.prepare(g, vw, s, L);
     const uint32_t n = P.view.n;
     P.uniform = P.view.n_active == 0 ? 0.0 : 1.0 / (double)P.view.n_active;
-    if (in.weight.present() && in.precision == GTC_PREC_F32 && !P.view.filtered)
-        P.wc = &weight_cache(g, in.weight, s, L);
+    if (in.weight.present()) {
+        const unsigned long long h = scan_weights(in.weight, g->m, s, L);
+        if (in.precision == GTC_PREC_F32 && !P.view.filtered) P.wc = &weight_cache(g, in.weight, h);
+    }
     if (need_deg && P.wc) {
         cached_degrees(g, *P.wc, P.view.reversed ? 0 : 1, s, L, &P.degp, &P.sinkp);
     } else if (need_deg) {

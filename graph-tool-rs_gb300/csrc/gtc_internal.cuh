@@ -171,9 +171,10 @@ struct BatchKey {
     int odt = -1;
     double d = 0.0, eps = 0.0;
     uint64_t max_iter = 0;
+    uint64_t sweep_limit = 0;
     bool operator==(const BatchKey& o) const {
         return w == o.w && wdt == o.wdt && out == o.out && odt == o.odt && d == o.d &&
-               eps == o.eps && max_iter == o.max_iter;
+               eps == o.eps && max_iter == o.max_iter && sweep_limit == o.sweep_limit;
     }
 };
 }  // namespace gtc
@@ -269,6 +270,11 @@ struct DVec {
     bool present() const { return p != nullptr; }
 };
 
+// One read of a weight map by EdgeId: its content hash; GTC_ERR_ARG if it
+// holds a non-finite value (gtc_centrality.cu).
+unsigned long long scan_weights(const DVec& w, uint64_t m, cudaStream_t s, uint64_t* launches);
+
+
 // One solve's inputs, after the C ABI checked them.  Every vector is in
 // device memory.
 struct SolveIn {
@@ -332,6 +338,10 @@ struct PprIn {
 };
 void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* res,
                cudaStream_t s);
+
+// One read of a weight map by EdgeId: its content hash; GTC_ERR_ARG if it
+// holds a non-finite value (gtc_centrality.cu).
+unsigned long long scan_weights(const DVec& w, uint64_t m, cudaStream_t s, uint64_t* launches);
 
 // solves (gtc_centrality.cu)
 void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc_result* res,

@@ -974,6 +974,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
         GTC_REQUIRE(in.seed_vertices[k] < n, GTC_ERR_INDEX, "a seed vertex is outside the vertex bound");
     const uint32_t ns = (uint32_t)ns_all;
 
+    if (in.weight.present()) (void)scan_weights(in.weight, g->m, s, &L);
     // degrees of the view and pull-ordered weights
     DevBuf<double> deg(n, s);
     if (n) {

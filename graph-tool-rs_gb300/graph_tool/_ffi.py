@@ -124,6 +124,7 @@ SIGNATURES = {
     "gtc_graph_batch_create": (C.c_int, [C.c_uint64, u64p, u64p, u32p, u32p,
                                          C.POINTER(C.c_void_p)]),
     "gtc_graph_batch_destroy": (C.c_int, [C.c_void_p]),
+    "gtc_debug_set_batch_sweep_limit": (C.c_int, [C.c_uint64]),
     "gtc_graph_batch_info": (C.c_int, [C.c_void_p, u64p, u64p, u64p]),
     "gtc_pagerank_batch": (C.c_int, [C.c_void_p, f64p, C.c_uint64, C.c_double, C.c_double,
                                      C.c_uint64, f64p, C.c_uint64, u64p, C.POINTER(Options),

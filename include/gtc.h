@@ -397,6 +397,12 @@ int gtc_pagerank_batch(gtc_graph_batch* b, const double* weight, uint64_t weight
                        uint64_t rank_len, uint64_t* iters, const gtc_options* opt,
                        gtc_result* result);
 
+/* Test hook: the number of sweeps after which an uncapped batch solve
+ * (max_iter 0) gives up with GTC_ERR_TIMEOUT (0 restores the default,
+ * 100,000).  It lets a test reach the timeout path in a few sweeps.
+ * Process-wide; not for use while batch solves run. */
+int gtc_debug_set_batch_sweep_limit(uint64_t limit);
+
 /* As gtc_pagerank_batch with weight and rank in device memory (FP32 or
  * FP64); iters stays a host array. */
 int gtc_pagerank_batch_device(gtc_graph_batch* b, const gtc_dvec* weight, double damping,
