@@ -157,6 +157,7 @@ struct PprSched {
     DevBuf<uint4> items;
     DevBuf<uint4> longs;    // {row, first chunk, chunks, 0}
     uint32_t n_items = 0, n_chunks = 0, n_long = 0;
+    uint32_t n_empty = 0;  // single rows without pull entries (the last items)
     bool built = false;
 };
 

@@ -6,11 +6,21 @@
 // each stopping at the first sweep whose L1 change falls below epsilon
 // (centrality.rs:372-381), its value the iterate of that sweep.
 //
-// Layout.  Z is [n x S] row-major, S = 32 * C slots (C = 1-4, 6, 8, 12 or 16
-// lines of 128 bytes); a warp reads a row with C / V coalesced vector loads
-// of V floats per lane (Lanes<C>).  Z[v][j]
-// holds rank_b[v] / deg_v of the column b in slot j for a vertex with
-// out-edges, and rank_b[v] itself for a sink (a sink is never gathered).
+// Layout.  Z is [n x P] row-major with a pitch P fixed for the whole call
+// (32 slots per line, lines for all B columns); a sweep uses the first S =
+// 32 * C slots of each row (C = 1-4, 6, 8, 12 or 16 lines of 128 bytes), and
+// a warp reads them with C / V coalesced vector loads of V floats per lane
+// (Lanes<C>).  Z[v][j] holds rank_b[v] / deg_v of the column b in slot j
+// for a vertex with out-edges, and rank_b[v] itself for a sink (a sink is
+// never gathered).
+//
+// Rows without in-edges.  A vertex with no in-edge that is no column's seed
+// has rank 0 in every column at every sweep ((1 - d) * 0 + d * (mass * 0 +
+// an empty sum)), and so does its change; both iterate buffers start zeroed
+// and the sweeps skip these rows (about half the vertices of an R-MAT
+// graph).  The fixed pitch keeps a skipped row's slots at zero when the
+// active columns are repacked.  Seeds without in-edges are finished by the
+// sweep's second kernel with an empty sum.
 //
 // Active columns only.  Columns converge at very different sweeps (for an
 // R-MAT graph and seed sets of 1-64 vertices the last column takes ~2.5x the
@@ -61,15 +71,18 @@ constexpr uint32_t PPR_NONE = 0xFFFFFFFFu;
 constexpr uint32_t PPR_HANDOFF = 8;
 
 struct PprArgs {
-    uint32_t n, s_in, s_out;             // slots per row of zin and zout
+    uint32_t n, s_in, s_out;             // slots used per row of zin and zout
+    uint32_t pitch;                      // floats per row of zin and zout
     const uint4* __restrict__ items;     // chunks, then single rows
     uint32_t n_items, n_chunks;
     const uint4* __restrict__ longs;     // {row, first chunk, chunks, 0}
     uint32_t n_long;
+    const uint32_t* __restrict__ eseeds; // seed rows without in-edges
+    uint32_t n_eseeds;
     const uint32_t* __restrict__ other;
     const float* __restrict__ w;         // pull-ordered weights or null
-    const float* __restrict__ zin;       // [n][s_in]
-    float* __restrict__ zout;            // [n][s_out]
+    const float* __restrict__ zin;       // [n][pitch], slots [0, s_in) used
+    float* __restrict__ zout;            // [n][pitch], slots [0, s_out) written
     const float2* __restrict__ dinv;     // {FP32 out-degree, its inverse}; {-1, 0} for a sink
     const uint32_t* __restrict__ seed_off;  // per vertex: seeds [seed_off[v], seed_off[v+1])
     const uint2* __restrict__ seeds;        // {column, float bits of the value}
@@ -203,7 +216,7 @@ __device__ __forceinline__ void gather(const PprArgs& A, uint32_t pb, uint32_t p
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const uint32_t src = __shfl_sync(0xffffffffu, my, (k + u) & 31);
-                if (k + u < cnt) Lanes<C>::template load<true>(A.zin + (size_t)src * A.s_in, lane, v[u]);
+                if (k + u < cnt) Lanes<C>::template load<true>(A.zin + (size_t)src * A.pitch, lane, v[u]);
             }
             float t[C];
 #pragma unroll
@@ -234,7 +247,7 @@ struct RowIn {
         dd = A.dinv[v];
         sb = A.seed_off[v];
         se = A.seed_off[v + 1];
-        Lanes<C>::template load<true>(A.zin + (size_t)v * A.s_in, lane, z);
+        Lanes<C>::template load<true>(A.zin + (size_t)v * A.pitch, lane, z);
     }
 };
 
@@ -258,26 +271,34 @@ __device__ __forceinline__ void finish_row(const PprArgs& A, uint32_t v, const R
                                            const float (&sum)[C], int lane, float2* dz,
                                            float2* sk, float* stage) {
     const bool snk = r.dd.x < 0.f;
+    const bool seeded = r.se > r.sb;
 #pragma unroll
     for (int q = 0; q < C; ++q) {
         const uint32_t j = Lanes<C>::slot(lane, q);
         const uint32_t os = __ldg(A.out_slot + j);
         if (os == PPR_NONE) continue;
-        const uint32_t col = __ldg(A.col_in + j);
         const float prev = snk ? r.z[q] : __fmul_rn(r.z[q], r.dd.x);
-        float pv = 0.f;
-        for (uint32_t t = r.sb; t < r.se; ++t) {
-            const uint2 sd = A.seeds[t];
-            if (sd.x == col) pv = __uint_as_float(sd.y);
+        float nv;
+        if (!seeded) {
+            // no seed in any column: pv = 0, where the general form below
+            // gives x = 0 + sum = sum and nv = 0 + d x, bit for bit
+            nv = __fmul_rn(A.d, sum[q]);
+        } else {
+            const uint32_t col = __ldg(A.col_in + j);
+            float pv = 0.f;
+            for (uint32_t t = r.sb; t < r.se; ++t) {
+                const uint2 sd = A.seeds[t];
+                if (sd.x == col) pv = __uint_as_float(sd.y);
+            }
+            const float x = __fadd_rn(__fmul_rn(__ldg(A.psink + j), pv), sum[q]);
+            nv = __fadd_rn(__fmul_rn(A.one_minus_d, pv), __fmul_rn(A.d, x));
         }
-        const float x = __fadd_rn(__fmul_rn(__ldg(A.psink + j), pv), sum[q]);
-        const float nv = __fadd_rn(__fmul_rn(A.one_minus_d, pv), __fmul_rn(A.d, x));
         smem_kahan_add(dz + 32 * q + lane, fabsf(__fsub_rn(nv, prev)));
         if (snk) smem_kahan_add(sk + 32 * q + lane, nv);
         stage[os] = snk ? nv : __fmul_rn(nv, r.dd.y);
     }
     __syncwarp();
-    float* zn = A.zout + (size_t)v * A.s_out + lane;
+    float* zn = A.zout + (size_t)v * A.pitch + lane;
     for (uint32_t j = 0; j < A.s_out; j += 32) zn[j] = stage[j + lane];
     __syncwarp();
 }
@@ -501,7 +522,7 @@ __global__ void __launch_bounds__(PB_NT) k_ppr_bulk(PprArgs A) {
             if (lane == 0) mbar_expect(bar, bB.cnt * (uint32_t)(S * 4));
             __syncwarp();
             if ((uint32_t)lane < bB.cnt)
-                bulk_g2s(smem_u32(ring + (size_t)(hB * BT + lane) * S), A.zin + (size_t)iA * S,
+                bulk_g2s(smem_u32(ring + (size_t)(hB * BT + lane) * S), A.zin + (size_t)iA * A.pitch,
                          S * 4, bar);
         }
         if (bB.valid && bB.first && bB.it >= A.n_chunks) rB.load(A, bB.v, lane);
@@ -591,7 +612,8 @@ __global__ void __launch_bounds__(PB_NT) k_ppr_bulk(PprArgs A) {
     }
 }
 
-// Sweep, part 2: every long row, its chunks' partials merged in chunk order.
+// Sweep, part 2: every long row, its chunks' partials merged in chunk order,
+// then every seed row without in-edges.
 template <int C>
 __global__ void __launch_bounds__(PPR_NT) k_ppr_long(PprArgs A) {
     extern __shared__ float2 ppr_sm[];
@@ -615,6 +637,16 @@ __global__ void __launch_bounds__(PPR_NT) k_ppr_long(PprArgs A) {
 #pragma unroll
         for (int q = 0; q < C; ++q) sum[q] = t[q].value();
         finish_row<C>(A, lr.x, r, sum, lane, m.dz, m.sk, m.stage);
+    }
+    // seed rows without in-edges: an empty sum
+    for (uint32_t k = gw; k < A.n_eseeds; k += nw) {
+        const uint32_t v = A.eseeds[k];
+        RowIn<C> r;
+        r.load(A, v, lane);
+        float sum[C];
+#pragma unroll
+        for (int q = 0; q < C; ++q) sum[q] = 0.f;
+        finish_row<C>(A, v, r, sum, lane, m.dz, m.sk, m.stage);
     }
     cta_fold<C>(A, m);
 }
@@ -676,14 +708,18 @@ __global__ void k_ppr_seed_off(uint32_t n, uint32_t ns, const uint32_t* __restri
 }
 
 // Internal label and degree of each seed vertex.
+// Internal label, degree and number of pull entries (in-edges) of each seed
+// vertex.
 __global__ void k_ppr_seed_lookup(uint32_t ns, const uint32_t* __restrict__ orig,
                                   const uint32_t* __restrict__ iperm, const double* __restrict__ deg,
-                                  uint32_t* __restrict__ iv, double* __restrict__ dv) {
+                                  const uint32_t* __restrict__ pull_off, uint32_t* __restrict__ iv,
+                                  double* __restrict__ dv, uint32_t* __restrict__ din) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ns) return;
     const uint32_t v = iperm[orig[k]];
     iv[k] = v;
     dv[k] = deg[v];
+    din[k] = pull_off[v + 1] - pull_off[v];
 }
 
 // out[col][perm i] = rank of column col at internal vertex i, for K
@@ -748,13 +784,15 @@ __global__ void k_gather_w_ppr(uint32_t m, const uint32_t* __restrict__ eid,
 }
 
 // schedule keys: 0 for a row cut into chunks, else PPR_CHUNK + 1 - in-degree
+// (cnt[0]: rows cut into chunks, cnt[1]: rows without pull entries)
 __global__ void k_ppr_keys(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ key,
-                           unsigned* __restrict__ n_long) {
+                           unsigned* __restrict__ cnt) {
     const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
     const uint32_t dg = off[v + 1] - off[v];
     key[v] = dg > PPR_CHUNK ? 0u : PPR_CHUNK + 1 - dg;
-    if (dg > PPR_CHUNK) atomicAdd(n_long, 1u);
+    if (dg > PPR_CHUNK) atomicAdd(cnt, 1u);
+    if (dg == 0) atomicAdd(cnt + 1, 1u);
 }
 
 __global__ void k_ppr_row_items(uint32_t k, const uint32_t* __restrict__ pos,
@@ -774,17 +812,18 @@ void build_ppr_schedule(gtc_graph* g, const View& view, cudaStream_t s, PprSched
     GTC_CUDA(cudaStreamSynchronize(s));
     uint64_t L = 0;
     DevBuf<uint32_t> key(n, h), skey(n, h), pos(n, h);
-    DevBuf<unsigned> cnt(1, h);
-    GTC_CUDA(cudaMemsetAsync(cnt.get(), 0, sizeof(unsigned), h));
+    DevBuf<unsigned> cnt(2, h);
+    GTC_CUDA(cudaMemsetAsync(cnt.get(), 0, 2 * sizeof(unsigned), h));
     if (n) {
         k_ppr_keys<<<grid_for(n, 256, 1u << 30), 256, 0, h>>>(n, view.pull_off, key.get(), cnt.get());
         GTC_LAUNCHED();
         L++;
         sort_positions_by_key(key.get(), n, PPR_CHUNK + 2, skey.get(), pos.get(), h, &L);
     }
-    unsigned n_long = 0;
-    GTC_CUDA(cudaMemcpyAsync(&n_long, cnt.get(), sizeof(unsigned), cudaMemcpyDeviceToHost, h));
+    unsigned cnts[2] = {0, 0};
+    GTC_CUDA(cudaMemcpyAsync(cnts, cnt.get(), 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, h));
     GTC_CUDA(cudaStreamSynchronize(h));
+    const unsigned n_long = cnts[0];
     std::vector<uint4> lrec(n_long);
     if (n_long) {
         DevBuf<uint4> drec(n_long, h);
@@ -808,6 +847,7 @@ void build_ppr_schedule(gtc_graph* g, const View& view, cudaStream_t s, PprSched
     S.n_long = n_long;
     S.n_chunks = (uint32_t)chunks.size();
     S.n_items = S.n_chunks + n_single;
+    S.n_empty = cnts[1];  // the last single rows (the highest key)
     S.items.alloc(S.n_items, h);
     S.longs.alloc(S.n_long, h);
     if (S.n_chunks)
@@ -1002,20 +1042,32 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
 
     // the seeds: internal labels, one record per (vertex, column) -- the
     // last value given for a pair wins -- sorted by vertex
-    std::vector<uint32_t> iv(ns);
+    std::vector<uint32_t> iv(ns), inn(ns);
     std::vector<double> dv(ns);
     if (ns) {
-        DevBuf<uint32_t> dorig(ns, s), div(ns, s);
+        DevBuf<uint32_t> dorig(ns, s), div(ns, s), dinn(ns, s);
         DevBuf<double> ddv(ns, s);
         GTC_CUDA(cudaMemcpyAsync(dorig.get(), in.seed_vertices, (size_t)ns * 4, cudaMemcpyHostToDevice, s));
-        k_ppr_seed_lookup<<<grid_for(ns, TB, 1u << 30), TB, 0, s>>>(ns, dorig.get(), g->iperm.get(),
-                                                                    deg.get(), div.get(), ddv.get());
+        k_ppr_seed_lookup<<<grid_for(ns, TB, 1u << 30), TB, 0, s>>>(
+            ns, dorig.get(), g->iperm.get(), deg.get(), view.pull_off, div.get(), ddv.get(), dinn.get());
         GTC_LAUNCHED();
         L++;
         GTC_CUDA(cudaMemcpyAsync(iv.data(), div.get(), (size_t)ns * 4, cudaMemcpyDeviceToHost, s));
         GTC_CUDA(cudaMemcpyAsync(dv.data(), ddv.get(), (size_t)ns * 8, cudaMemcpyDeviceToHost, s));
+        GTC_CUDA(cudaMemcpyAsync(inn.data(), dinn.get(), (size_t)ns * 4, cudaMemcpyDeviceToHost, s));
         GTC_CUDA(cudaStreamSynchronize(s));
     }
+    // seed rows without in-edges (the sweeps' single rows skip every row
+    // without in-edges), ascending
+    std::vector<uint32_t> hes;
+    for (uint32_t k = 0; k < ns; ++k)
+        if (inn[k] == 0) hes.push_back(iv[k]);
+    std::sort(hes.begin(), hes.end());
+    hes.erase(std::unique(hes.begin(), hes.end()), hes.end());
+    const uint32_t n_es = (uint32_t)hes.size();
+    DevBuf<uint32_t> des(n_es ? n_es : 1, s);
+    if (n_es)
+        GTC_CUDA(cudaMemcpyAsync(des.get(), hes.data(), (size_t)n_es * 4, cudaMemcpyHostToDevice, s));
     struct Rec {
         uint32_t v, col;
         float val;
@@ -1057,10 +1109,11 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     GTC_LAUNCHED();
     L++;
 
-    // iterates: the first layout is slot = column
+    // iterates: the first layout is slot = column; the row pitch stays P
     uint32_t C = ppr_lines(B);
     uint32_t s_in = 32 * C;
-    const size_t zn = (size_t)n * s_in;
+    const uint32_t P = s_in;
+    const size_t zn = (size_t)n * P;
     // the two iterate buffers live on the handle: a later batch of the same
     // or a smaller width does not allocate them again
     if (g->ppr_z[0].n < zn || !g->ppr_z[0].get()) {
@@ -1071,7 +1124,10 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     }
     DevBuf<float>& z0 = g->ppr_z[0];
     DevBuf<float>& z1 = g->ppr_z[1];
-    if (zn) GTC_CUDA(cudaMemsetAsync(z0.get(), 0, zn * sizeof(float), s));
+    if (zn) {
+        GTC_CUDA(cudaMemsetAsync(z0.get(), 0, zn * sizeof(float), s));
+        GTC_CUDA(cudaMemsetAsync(z1.get(), 0, zn * sizeof(float), s));
+    }
     if (nu && n) {
         k_ppr_init<<<grid_for(nu, TB, 1u << 30), TB, 0, s>>>(nu, s_in, dsv.get(), dsd.get(),
                                                              dinv.get(), z0.get());
@@ -1083,7 +1139,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const unsigned grid1_max = (unsigned)sms * (2048 / 32);  // at most one CTA per warp slot
     const unsigned grid2 =
-        std::max(1u, std::min((S.n_long + PPR_WARPS - 1) / PPR_WARPS, (unsigned)sms));
+        std::max(1u, std::min((S.n_long + n_es + PPR_WARPS - 1) / PPR_WARPS, (unsigned)sms));
     DevBuf<float2> cpart((size_t)S.n_chunks * s_in, s);
     DevBuf<double> part((size_t)(grid1_max + grid2) * 2 * s_in, s), out(2 * (size_t)s_in, s);
     DevBuf<uint32_t> dmap(2 * (size_t)s_in, s);  // col_in, then out_slot
@@ -1095,8 +1151,10 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
 
     PprArgs A{};
     A.n = n;
-    A.items = S.items.get(), A.n_items = S.n_items, A.n_chunks = S.n_chunks;
+    A.pitch = P;
+    A.items = S.items.get(), A.n_items = S.n_items - S.n_empty, A.n_chunks = S.n_chunks;
     A.longs = S.longs.get(), A.n_long = S.n_long;
+    A.eseeds = des.get(), A.n_eseeds = n_es;
     A.other = view.pull_other, A.w = wpull.get();
     A.dinv = dinv.get();
     A.seed_off = dso.get(), A.seeds = dsd.get();
@@ -1179,7 +1237,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
             GTC_CUDA(cudaMemcpyAsync(dpairs.get(), store.data(), K * sizeof(uint2),
                                      cudaMemcpyHostToDevice, s));
             dim3 g2((n + 31) / 32, (K + 31) / 32), blk(32, 8);
-            k_ppr_store<<<g2, blk, 0, s>>>(n, s_out, K, dpairs.get(), g->perm.get(), dinv.get(), zx,
+            k_ppr_store<<<g2, blk, 0, s>>>(n, P, K, dpairs.get(), g->perm.get(), dinv.get(), zx,
                                           in.out, in.out_dtype);
             GTC_LAUNCHED();
             L++;
@@ -1201,7 +1259,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
                 const uint2 pair = make_uint2(j, c);
                 GTC_CUDA(cudaMemcpyAsync(dpairs.get(), &pair, sizeof(uint2), cudaMemcpyHostToDevice, s));
                 dim3 g2((n + 31) / 32, 1), blk(32, 8);
-                k_ppr_store<<<g2, blk, 0, s>>>(n, s_in, 1, dpairs.get(), g->perm.get(), dinv.get(),
+                k_ppr_store<<<g2, blk, 0, s>>>(n, P, 1, dpairs.get(), g->perm.get(), dinv.get(),
                                               zc, in.out, in.out_dtype);
                 GTC_LAUNCHED();
                 const uint64_t sb = in.seed_off[c], se = in.seed_off[c + 1];

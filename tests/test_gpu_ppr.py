@@ -17,9 +17,10 @@ def _seed_sets(n, B, rng, max_size=8):
 
 
 def _check(oracle, gtc, n, src, tgt, B, weight=None, reversed=False, eps=1e-7, seed=1,
-           gather="bulk"):
+           gather="bulk", sets=None):
     rng = np.random.default_rng(seed)
-    sets = _seed_sets(n, B, rng)
+    if sets is None:
+        sets = _seed_sets(n, B, rng)
     g = gtc.Graph()
     g.add_vertex(n)
     g.add_edges(src, tgt)
@@ -75,6 +76,26 @@ def test_ppr_batch_reversed_with_hubs(oracle, gtc, variant):
            gather=variant)
     _check(oracle, gtc, n, src.astype(np.uint32), tgt.astype(np.uint32), 64, seed=7, reversed=True,
            gather=variant)
+
+
+def test_ppr_batch_seeds_without_in_edges(oracle, gtc, variant):
+    # The sweeps skip rows without in-edges; seeds among them (sinks and
+    # vertices with out-edges) are finished with an empty sum, and the
+    # skipped rows must read as zero after the columns are repacked.
+    from graph_tool import synth
+    n, src, tgt = synth.rmat_cpu(10, edge_factor=8, seed=9)
+    indeg = np.bincount(tgt, minlength=n)
+    outdeg = np.bincount(src, minlength=n)
+    no_in = np.flatnonzero(indeg == 0)
+    no_in_src = np.flatnonzero((indeg == 0) & (outdeg > 0))
+    assert no_in.size > 100 and no_in_src.size > 10
+    rng = np.random.default_rng(11)
+    sets = []
+    for b in range(70):
+        k = int(rng.integers(1, 6))
+        pool = no_in_src if b % 3 == 0 else (no_in if b % 3 == 1 else np.arange(n))
+        sets.append(rng.choice(pool, min(k, pool.size), replace=False))
+    _check(oracle, gtc, n, src, tgt, len(sets), gather=variant, sets=sets)
 
 
 def test_ppr_batch_max_iter_caps_every_column(oracle, gtc, variant):
