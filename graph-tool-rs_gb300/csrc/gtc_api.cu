@@ -585,7 +585,6 @@ int gtc_ppr_batch(gtc_graph* g, const gtc_view* view, const double* weight, uint
 static void destroy_batch(gtc_graph_batch* b) {
     if (!b) return;
     if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->side) cudaStreamDestroy(b->side);
     gtc_graph* u = b->u;
     b->u = nullptr;
     delete b;  // its buffers are freed on the union's home stream

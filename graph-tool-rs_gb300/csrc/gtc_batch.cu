@@ -16,18 +16,19 @@
 // (sliced ELL), so lane i of a warp sums row i of a slice and every load of
 // the entry stream is one coalesced line.  Slices never cross graphs.
 //
-// Persistent kernels solve the graphs: a worker takes the next graph
-// (largest first, through an atomic work counter) and runs its whole power
-// iteration -- sweeps separated by CTA or cluster barriers only, no
-// grid-wide barrier -- before it takes another.  Graphs of up to GB_CL_CAP
-// vertices are solved by one CTA and graphs of up to 2 * GB_CL_CAP by a
-// cluster of two, with the gathered vector x = rank / out-degree in shared
-// memory (k_pr_graphs_cl); larger graphs go to one CTA that gathers from
-// global memory (k_pr_graphs_gl), launched beside it on a second stream.  A
-// graph's rows are assigned and its sums folded in a fixed order, so its
-// result does not depend on which worker took it.  The solve's launches
-// (weight gathers, degrees, both kernels) are captured once into a CUDA
-// graph and replayed while the inputs keep their addresses.
+// One persistent kernel (k_pr_graphs) solves the graphs: a worker takes the
+// next graph (largest first, through an atomic work counter per queue) and
+// runs its whole power iteration -- sweeps separated by CTA or cluster
+// barriers only, no grid-wide barrier -- before it takes another.  Its
+// workers are clusters of two CTAs.  Graphs larger than 2 * GB_CL_CAP
+// vertices come first, a CTA each, gathering x = rank / out-degree from
+// global memory; then graphs of up to 2 * GB_CL_CAP vertices, a cluster each,
+// with half of x in each CTA's shared memory; then graphs of up to GB_CL_CAP
+// vertices, a CTA each, with x in its shared memory.  A graph's rows are
+// assigned and its sums folded in a fixed order, so its result does not
+// depend on which worker took it.  The solve's launches (weight gathers,
+// degrees, the kernel) are captured once into a CUDA graph and replayed
+// while the inputs keep their addresses.
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
@@ -348,13 +349,16 @@ __device__ __forceinline__ void solve_graph(const GbArgs& A, uint32_t gk, float*
     if ((MODE != GB_PAIR || r == 0) && threadIdx.x == 0) A.iters[gk] = it;
 }
 
-// The pair queue, then the single queue.  A cluster takes pair graphs
-// (rank 0 draws from the counter and its peer reads the draw from rank 0's
-// shared memory) until the queue is empty; from then on each CTA draws
-// single graphs alone, with no cluster barrier and no access to the peer's
-// shared memory, so the CTAs of a cluster may finish at different times.
+// The global queue, the pair queue, then the single queue.  Each CTA
+// first draws global graphs alone.  Then a cluster takes pair graphs (rank
+// 0 draws from the counter and its peer reads the draw from rank 0's shared
+// memory) until the queue is empty; the first draw waits for both CTAs, so a
+// CTA whose peer still solves a global graph waits for it.  From then on
+// each CTA draws single graphs alone, with no cluster barrier and no access
+// to the peer's shared memory, so the CTAs of a cluster may finish at
+// different times.
 template <bool W>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_NT, 1) k_pr_graphs_cl(GbArgs A) {
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_NT, 1) k_pr_graphs(GbArgs A) {
     extern __shared__ float ys[];
     __shared__ double2 sm[GB_WARPS + 1];
     __shared__ double2 part;
@@ -364,6 +368,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_NT, 1) k_pr_graph
     const float* ypeer = cl.map_shared_rank(ys, r ^ 1u);
     const double2* ppeer = cl.map_shared_rank(&part, r ^ 1u);
     const uint32_t* graph0 = cl.map_shared_rank(&s_graph, 0u);
+    for (;;) {
+        if (threadIdx.x == 0) s_graph = atomicAdd(A.counter + 2, 1u);
+        __syncthreads();
+        const uint32_t k = s_graph;
+        __syncthreads();
+        if (k >= A.n_global) break;
+        solve_graph<W, GB_GLOBAL>(A, A.order[A.n_pair + A.n_single + k], nullptr, nullptr, 0, sm,
+                                  nullptr, nullptr);
+    }
     for (;;) {
         if (r == 0 && threadIdx.x == 0) s_graph = atomicAdd(A.counter, 1u);
         cl.sync();
@@ -379,22 +392,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_NT, 1) k_pr_graph
         __syncthreads();
         if (k >= A.n_single) return;
         solve_graph<W, GB_SINGLE>(A, A.order[A.n_pair + k], ys, nullptr, 0, sm, nullptr, nullptr);
-    }
-}
-
-// The global queue: graphs whose halves exceed a CTA's shared memory.
-template <bool W>
-__global__ void __launch_bounds__(GB_NT, 1) k_pr_graphs_gl(GbArgs A) {
-    __shared__ double2 sm[GB_WARPS + 1];
-    __shared__ uint32_t s_graph;
-    for (;;) {
-        if (threadIdx.x == 0) s_graph = atomicAdd(A.counter + 2, 1u);
-        __syncthreads();
-        const uint32_t k = s_graph;
-        __syncthreads();
-        if (k >= A.n_global) return;
-        solve_graph<W, GB_GLOBAL>(A, A.order[A.n_pair + A.n_single + k], nullptr, nullptr, 0, sm,
-                                  nullptr, nullptr);
     }
 }
 
@@ -694,35 +691,25 @@ void pagerank_batch(gtc_graph_batch* b, const DVec& weight, double damping, doub
             cudaGraphExecDestroy(b->exec);
             b->exec = nullptr;
         }
-        int sms = 0, dev = 0, per_sm = 0;
+        int sms = 0, dev = 0;
         GTC_CUDA(cudaGetDevice(&dev));
         GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        void (*kern_cl)(GbArgs) = W ? k_pr_graphs_cl<true> : k_pr_graphs_cl<false>;
-        void (*kern_gl)(GbArgs) = W ? k_pr_graphs_gl<true> : k_pr_graphs_gl<false>;
-        const uint32_t n_cl = b->n_pair + b->n_single, n_big = b->n_global;
-        unsigned grid = 0, grid_cl = 0;
-        const size_t smem_cl = (size_t)std::max<uint32_t>(b->smem_floats, 1u) * sizeof(float);
-        if (n_cl) {
-            GTC_CUDA(cudaFuncSetAttribute(kern_cl, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem_cl));
+        void (*kern)(GbArgs) = W ? k_pr_graphs<true> : k_pr_graphs<false>;
+        const uint32_t n_graphs = b->n_pair + b->n_single + b->n_global;
+        unsigned grid = 0;
+        const size_t smem = (size_t)std::max<uint32_t>(b->smem_floats, 1u) * sizeof(float);
+        if (n_graphs) {
+            GTC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             cudaLaunchConfig_t cfg{};
             cfg.gridDim = dim3(2 * (unsigned)sms);
             cfg.blockDim = dim3(GB_NT);
-            cfg.dynamicSmemBytes = smem_cl;
+            cfg.dynamicSmemBytes = smem;
             int clusters = 0;
-            GTC_CUDA(cudaOccupancyMaxActiveClusters(&clusters, kern_cl, &cfg));
-            const uint32_t useful = b->n_pair + (b->n_single + 1) / 2;
-            grid_cl = 2u * (unsigned)std::max(1, std::min<int>(clusters, (int)useful));
-        }
-        if (n_big) {
-            GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern_gl, GB_NT, 0));
-            grid = (unsigned)std::max(1, std::min<int>(sms * std::max(per_sm, 1), (int)n_big));
-            if (!b->side) GTC_CUDA(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
-        }
-        cudaEvent_t fork = nullptr, join = nullptr;
-        if (n_big) {
-            GTC_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
-            GTC_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+            GTC_CUDA(cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg));
+            // every cluster that can have work: a pair graph, or two graphs of
+            // the other queues
+            const uint32_t useful = b->n_pair + (b->n_single + b->n_global + 1) / 2;
+            grid = 2u * (unsigned)std::max(1, std::min<int>(clusters, (int)useful));
         }
         cudaGraph_t graph = nullptr;
         GTC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -766,25 +753,16 @@ void pagerank_batch(gtc_graph_batch* b, const DVec& weight, double damping, doub
         A.out_dtype = out_dtype;
         A.iters = b->iters.get();
         A.counter = b->counter.get();
-        if (n_big) {  // the graphs too large for shared memory, beside the others
-            cudaEventRecord(fork, s);
-            cudaStreamWaitEvent(b->side, fork, 0);
-            kern_gl<<<grid, GB_NT, 0, b->side>>>(A);
-            cudaEventRecord(join, b->side);
-        }
-        if (n_cl) kern_cl<<<grid_cl, GB_NT, smem_cl, s>>>(A);
-        if (n_big) cudaStreamWaitEvent(s, join, 0);
+        if (n_graphs) kern<<<grid, GB_NT, smem, s>>>(A);
         const cudaError_t ce = cudaStreamEndCapture(s, &graph);
         GTC_CUDA(ce);
         GTC_LAUNCHED();
-        if (fork) cudaEventDestroy(fork);
-        if (join) cudaEventDestroy(join);
         const cudaError_t ie = cudaGraphInstantiate(&b->exec, graph, 0);
         cudaGraphDestroy(graph);
         GTC_CUDA(ie);
         b->key = key;
         b->launches_per_solve =
-            (W && m ? 1 : 0) + (W && b->n_lay ? 1 : 0) + (n ? 1 : 0) + (n_cl ? 1 : 0) + (n_big ? 1 : 0);
+            (W && m ? 1 : 0) + (W && b->n_lay ? 1 : 0) + (n ? 1 : 0) + (n_graphs ? 1 : 0);
     }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (timing) {

@@ -218,7 +218,6 @@ struct gtc_graph_batch {
     uint64_t n_lay = 0;
     uint32_t n_pair = 0, n_single = 0, n_global = 0;
     uint32_t smem_floats = 0;                // x entries a CTA of the first two queues holds
-    cudaStream_t side = nullptr;             // the global queue's stream while captured
     gtc::DevBuf<float> invdeg, r0, r1, y0, y1, wout;
     gtc::DevBuf<uint8_t> sink;
     gtc::DevBuf<uint64_t> iters;
