@@ -722,18 +722,21 @@ __global__ void k_ppr_seed_lookup(uint32_t ns, const uint32_t* __restrict__ orig
     din[k] = pull_off[v + 1] - pull_off[v];
 }
 
-// out[col][perm i] = rank of column col at internal vertex i, for K
-// (slot, column) pairs (transposed through shared memory).
+// out[col][o] = rank of column col at original vertex o (internal label
+// iperm[o]), for K (slot, column) pairs in slot order, transposed through
+// shared memory: a warp reads the 32 pairs' slots of one row (consecutive
+// slots share sectors) and writes 32 consecutive vertices of one column.
 __global__ void k_ppr_store(uint32_t n, uint32_t S, uint32_t K, const uint2* __restrict__ pairs,
-                            const uint32_t* __restrict__ perm, const float2* __restrict__ dinv,
+                            const uint32_t* __restrict__ iperm, const float2* __restrict__ dinv,
                             const float* __restrict__ z, void* __restrict__ out, int dt) {
     __shared__ float tile[32][33];
-    const uint32_t i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+    const uint32_t o0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
     const uint32_t tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
     for (uint32_t r = ty; r < 32; r += 8) {
-        const uint32_t i = i0 + r, k = k0 + tx;
+        const uint32_t o = o0 + r, k = k0 + tx;
         float val = 0.f;
-        if (i < n && k < K) {
+        if (o < n && k < K) {
+            const uint32_t i = iperm[o];
             const float zz = z[(size_t)i * S + pairs[k].x];
             const float2 dd = dinv[i];
             val = dd.x < 0.f ? zz : __fmul_rn(zz, dd.x);
@@ -742,13 +745,13 @@ __global__ void k_ppr_store(uint32_t n, uint32_t S, uint32_t K, const uint2* __r
     }
     __syncthreads();
     for (uint32_t r = ty; r < 32; r += 8) {
-        const uint32_t k = k0 + r, i = i0 + tx;
-        if (k < K && i < n) {
-            const size_t o = (size_t)pairs[k].y * n + perm[i];
+        const uint32_t k = k0 + r, o = o0 + tx;
+        if (k < K && o < n) {
+            const size_t at = (size_t)pairs[k].y * n + o;
             if (dt == GTC_F64)
-                ((double*)out)[o] = (double)tile[tx][r];
+                ((double*)out)[at] = (double)tile[tx][r];
             else
-                ((float*)out)[o] = tile[tx][r];
+                ((float*)out)[at] = tile[tx][r];
         }
     }
 }
@@ -1237,7 +1240,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
             GTC_CUDA(cudaMemcpyAsync(dpairs.get(), store.data(), K * sizeof(uint2),
                                      cudaMemcpyHostToDevice, s));
             dim3 g2((n + 31) / 32, (K + 31) / 32), blk(32, 8);
-            k_ppr_store<<<g2, blk, 0, s>>>(n, P, K, dpairs.get(), g->perm.get(), dinv.get(), zx,
+            k_ppr_store<<<g2, blk, 0, s>>>(n, P, K, dpairs.get(), g->iperm.get(), dinv.get(), zx,
                                           in.out, in.out_dtype);
             GTC_LAUNCHED();
             L++;
@@ -1259,7 +1262,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
                 const uint2 pair = make_uint2(j, c);
                 GTC_CUDA(cudaMemcpyAsync(dpairs.get(), &pair, sizeof(uint2), cudaMemcpyHostToDevice, s));
                 dim3 g2((n + 31) / 32, 1), blk(32, 8);
-                k_ppr_store<<<g2, blk, 0, s>>>(n, P, 1, dpairs.get(), g->perm.get(), dinv.get(),
+                k_ppr_store<<<g2, blk, 0, s>>>(n, P, 1, dpairs.get(), g->iperm.get(), dinv.get(),
                                               zc, in.out, in.out_dtype);
                 GTC_LAUNCHED();
                 const uint64_t sb = in.seed_off[c], se = in.seed_off[c + 1];
