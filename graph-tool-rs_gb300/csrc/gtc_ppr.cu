@@ -36,17 +36,24 @@
 // PPR_CHUNK entries; the first kernel of a sweep runs every chunk (a warp
 // each, partials to memory) and every other row (a warp each, heaviest
 // first), the second merges each long row's chunk partials in chunk order and
-// finishes it.  Assignments are fixed strides and every fold runs in a fixed
-// order, so the results do not depend on timing.
+// finishes it, the third sums the new iterate over the sink rows (the
+// dangling mass of the next sweep) and the fourth folds the CTAs' partials.
+// Assignments are fixed strides and every fold runs in a fixed order, so the
+// results do not depend on timing.
 //
 // Latency.  A warp loads its next work item while it works on the current
 // one, and a row's epilogue inputs (degree, seeds, previous values) are
 // loaded before its gathers, so a row costs one index load plus its gather
 // rounds on the critical path.
 //
-// Precision.  Row sums are FP32 with Kahan compensation; the L1 change and
-// dangling mass per column are accumulated per warp with Kahan compensation
-// in FP32 and folded over warps and CTAs in FP64.  The per-row work stays off
+// Precision.  Row sums are FP32 with Kahan compensation.  The L1 change per
+// column is one FP32 partial per slot and warp (a warp finishes about
+// n / 2,400 rows of a sweep; the rounding errors of its partial are
+// unbiased, so the total's relative error is about 1e-7 / sqrt(warps)),
+// folded over warps and CTAs in FP64; shared memory goes to the gather rings
+// instead (see pb_rows).  The dangling mass per column is summed with Kahan
+// compensation per warp from the new iterate's sink rows and folded in FP64.
+// The per-row work stays off
 // the FP64 pipe (on this GPU a few FP64 operations per row cost more than the
 // row's gathers): degrees and their inverses are precomputed in FP32.
 #include <algorithm>
@@ -73,6 +80,7 @@ constexpr uint32_t PPR_HANDOFF = 8;
 struct PprArgs {
     uint32_t n, s_in, s_out;             // slots used per row of zin and zout
     uint32_t pitch;                      // floats per row of zin and zout
+    uint32_t in_place;                   // out_slot[j] is j or PPR_NONE for every j
     const uint4* __restrict__ items;     // chunks, then single rows
     uint32_t n_items, n_chunks;
     const uint4* __restrict__ longs;     // {row, first chunk, chunks, 0}
@@ -251,31 +259,24 @@ struct RowIn {
     }
 };
 
-// Compensated FP32 accumulation into a shared-memory slot {s, c} (value s - c).
-__device__ __forceinline__ void smem_kahan_add(float2* acc, float x) {
-    float2 a = *acc;
-    const float y = __fsub_rn(x, a.y);
-    const float t = __fadd_rn(a.x, y);
-    a.y = __fsub_rn(__fsub_rn(t, a.x), y);
-    a.x = t;
-    *acc = a;
-}
-
-// Row v's new values for a lane's C input slots, written to zout in the
-// output layout through the warp's staging row (empty output slots stay 0);
-// the L1 change and dangling mass go to the warp's compensated accumulators,
-// held at position 32 q + lane for the lane's q-th slot (conflict-free).
-// Nothing here runs on the FP64 pipe.
+// Row v's new values for a lane's C input slots, stored to zout.  The L1
+// change goes to the warp's accumulator in shared memory (the lane's q-th
+// slot at 32 q + lane: conflict-free), one FP32 partial per slot and warp,
+// folded over warps and CTAs in FP64; the dangling mass is summed from zout
+// afterwards (k_ppr_sinks).  Nothing here runs on the FP64 pipe.
 template <int C>
 __device__ __forceinline__ void finish_row(const PprArgs& A, uint32_t v, const RowIn<C>& r,
-                                           const float (&sum)[C], int lane, float2* dz,
-                                           float2* sk, float* stage) {
+                                           const float (&sum)[C], int lane, float* dz) {
     const bool snk = r.dd.x < 0.f;
     const bool seeded = r.se > r.sb;
+    uint32_t osv[C];
+    float outv[C];
 #pragma unroll
     for (int q = 0; q < C; ++q) {
         const uint32_t j = Lanes<C>::slot(lane, q);
         const uint32_t os = __ldg(A.out_slot + j);
+        osv[q] = os;
+        outv[q] = 0.f;
         if (os == PPR_NONE) continue;
         const float prev = snk ? r.z[q] : __fmul_rn(r.z[q], r.dd.x);
         float nv;
@@ -293,52 +294,59 @@ __device__ __forceinline__ void finish_row(const PprArgs& A, uint32_t v, const R
             const float x = __fadd_rn(__fmul_rn(__ldg(A.psink + j), pv), sum[q]);
             nv = __fadd_rn(__fmul_rn(A.one_minus_d, pv), __fmul_rn(A.d, x));
         }
-        smem_kahan_add(dz + 32 * q + lane, fabsf(__fsub_rn(nv, prev)));
-        if (snk) smem_kahan_add(sk + 32 * q + lane, nv);
-        stage[os] = snk ? nv : __fmul_rn(nv, r.dd.y);
+        float* a = dz + 32 * q + lane;
+        *a = __fadd_rn(*a, fabsf(__fsub_rn(nv, prev)));
+        outv[q] = snk ? nv : __fmul_rn(nv, r.dd.y);
     }
-    __syncwarp();
-    float* zn = A.zout + (size_t)v * A.pitch + lane;
-    for (uint32_t j = 0; j < A.s_out; j += 32) zn[j] = stage[j + lane];
-    __syncwarp();
+    // In place (every sweep but those that repack the columns), each lane's
+    // V values go to its own input slots with vector stores, coalesced over
+    // the warp (a converged column's slot gets 0: no sweep reads it again);
+    // otherwise one store per computed slot.
+    float* zn = A.zout + (size_t)v * A.pitch;
+    constexpr int V = Lanes<C>::V;
+    if (A.in_place) {
+#pragma unroll
+        for (int t = 0; t < C / V; ++t) {
+            float* p = zn + Lanes<C>::slot(lane, V * t);
+            if (V == 4)
+                *reinterpret_cast<float4*>(p) =
+                    make_float4(outv[4 * t], outv[4 * t + 1], outv[4 * t + 2], outv[4 * t + 3]);
+            else if (V == 2)
+                *reinterpret_cast<float2*>(p) = make_float2(outv[2 * t], outv[2 * t + 1]);
+            else
+                *p = outv[t];
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < C; ++q)
+            if (osv[q] != PPR_NONE) zn[osv[q]] = outv[q];
+    }
 }
 
-// Shared memory of both kernels: per warp [s_in] compensated change and mass
-// and a staging row of s_in floats.
-inline size_t ppr_smem(uint32_t s_in) {
-    return (size_t)PPR_WARPS * s_in * (2 * sizeof(float2) + sizeof(float));
+// Shared memory of the register-gather and long-row kernels: per warp [s_in]
+// partial L1 changes.
+inline size_t ppr_smem(uint32_t s_in) { return (size_t)PPR_WARPS * s_in * sizeof(float); }
+
+// The warp's accumulator (zeroed).
+__device__ __forceinline__ float* warp_dz(float* sm, uint32_t s_in, int warp, int lane) {
+    float* dz = sm + (size_t)warp * s_in;
+    for (uint32_t j = lane; j < s_in; j += 32) dz[j] = 0.f;
+    __syncwarp();
+    return dz;
 }
 
-struct WarpSmem {
-    float2 *dz_all, *sk_all, *dz, *sk;
-    float* stage;
-    __device__ __forceinline__ WarpSmem(float2* sm, uint32_t s_in, int warp, int lane) {
-        dz_all = sm;
-        sk_all = sm + PPR_WARPS * s_in;
-        dz = dz_all + warp * s_in;
-        sk = sk_all + warp * s_in;
-        stage = reinterpret_cast<float*>(sk_all + PPR_WARPS * s_in) + warp * s_in;
-        for (uint32_t j = lane; j < s_in; j += 32)
-            dz[j] = make_float2(0.f, 0.f), sk[j] = make_float2(0.f, 0.f), stage[j] = 0.f;
-        __syncwarp();
-    }
-};
-
-// The CTA's per-slot sums (warps in order, FP64) into its partial record.
+// The CTA's per-slot L1 change (warps in order, FP64) into its partial record
+// {change per input slot, dangling mass per output slot (none here)}.
 template <int C>
-__device__ __forceinline__ void cta_fold(const PprArgs& A, const WarpSmem& m) {
+__device__ __forceinline__ void cta_fold(const PprArgs& A, const float* dz_all, int warps,
+                                         uint32_t warp_stride) {
     __syncthreads();
     double* dst = A.part + (size_t)(A.part_base + blockIdx.x) * 2 * A.s_in;
-    for (uint32_t pos = threadIdx.x; pos < A.s_in; pos += PPR_NT) {
-        double a = 0.0, b = 0.0;
-        for (int w = 0; w < PPR_WARPS; ++w) {
-            const float2 x = m.dz_all[w * A.s_in + pos], y = m.sk_all[w * A.s_in + pos];
-            a += (double)x.x - (double)x.y;
-            b += (double)y.x - (double)y.y;
-        }
-        const uint32_t j = Lanes<C>::slot(pos & 31, pos >> 5);
-        dst[j] = a;
-        dst[A.s_in + j] = b;
+    for (uint32_t pos = threadIdx.x; pos < A.s_in; pos += blockDim.x) {
+        double a = 0.0;
+        for (int w = 0; w < warps; ++w) a += (double)dz_all[(size_t)w * warp_stride + pos];
+        dst[Lanes<C>::slot(pos & 31, pos >> 5)] = a;
+        dst[A.s_in + pos] = 0.0;
     }
 }
 
@@ -347,9 +355,9 @@ __device__ __forceinline__ void cta_fold(const PprArgs& A, const WarpSmem& m) {
 // each next item while it works on the current one.
 template <int C, int U, bool W>
 __global__ void __launch_bounds__(PPR_NT) k_ppr_rows(PprArgs A) {
-    extern __shared__ float2 ppr_sm[];
+    extern __shared__ float ppr_sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const WarpSmem m(ppr_sm, A.s_in, warp, lane);
+    float* dz = warp_dz(ppr_sm, A.s_in, warp, lane);
     const uint32_t gw = blockIdx.x * PPR_WARPS + warp, nw = gridDim.x * PPR_WARPS;
     uint4 nxt = gw < A.n_items ? A.items[gw] : make_uint4(0u, 0u, 0u, 0u);
     for (uint32_t it = gw; it < A.n_items; it += nw) {
@@ -370,10 +378,10 @@ __global__ void __launch_bounds__(PPR_NT) k_ppr_rows(PprArgs A) {
             float sum[C];
 #pragma unroll
             for (int q = 0; q < C; ++q) sum[q] = __fsub_rn(acc.s[q], acc.c[q]);
-            finish_row<C>(A, cur.x, r, sum, lane, m.dz, m.sk, m.stage);
+            finish_row<C>(A, cur.x, r, sum, lane, dz);
         }
     }
-    cta_fold<C>(A, m);
+    cta_fold<C>(A, ppr_sm, PPR_WARPS, A.s_in);
 }
 
 
@@ -392,9 +400,13 @@ constexpr long long PB_WAIT_CYCLES = 4000000000ll;  // ~2 s: a copy that never l
 constexpr uint32_t PB_BLOCK = 8;                    // rows per plain partial sum
 
 // rows per batch: about 4 KB of rows, 2..32
-// rows per batch: 4 KB of rows (more, smaller rings keep more warps resident,
-// which measured faster than fewer warps with longer batches), 2..32
-constexpr int pb_rows(int C) { return 32 / C < 2 ? 2 : 32 / C; }
+// rows per batch: 6 KB of rows, 2..32.  The sweep is bound by the bytes of
+// rows in flight: four CTAs of four warps fit an SM (registers), and with
+// the per-warp accumulators at one float per slot each warp's ring holds
+// two batches of 6 KB in the same 54 KB a CTA had for 4 KB batches.  Per
+// 256-column sweep of an R-MAT-22 graph: 8.90 ms (4 KB), 8.21 (5 KB), 7.80
+// (6 KB); eight warps with 8 KB batches were slower than sixteen with 4 KB.
+constexpr int pb_rows(int C) { return 48 / C < 2 ? 2 : (48 / C > 32 ? 32 : 48 / C); }
 
 template <int C>
 struct PbLayout {
@@ -402,9 +414,8 @@ struct PbLayout {
     static constexpr int BT = pb_rows(C);
     static constexpr int RING = 2 * BT * S * 4;               // bytes
     static constexpr int DZ = RING + 16;                      // after the two mbarriers
-    static constexpr int SK = DZ + S * 8;
-    static constexpr int ST = SK + S * 8;
-    static constexpr int WARP = ((ST + S * 4) + 127) / 128 * 128;  // per-warp bytes
+    static constexpr int WARP = (DZ + S * 4 + 127) / 128 * 128;  // per-warp bytes
+    static constexpr int CTA = PB_WARPS * WARP;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -462,11 +473,8 @@ __global__ void __launch_bounds__(PB_NT) k_ppr_bulk(PprArgs A) {
     unsigned char* wsm = pb_sm + warp * Lay::WARP;
     float* ring = reinterpret_cast<float*>(wsm);
     const uint32_t bar0 = smem_u32(wsm + Lay::RING);
-    float2* dz = reinterpret_cast<float2*>(wsm + Lay::DZ);
-    float2* sk = reinterpret_cast<float2*>(wsm + Lay::SK);
-    float* stage = reinterpret_cast<float*>(wsm + Lay::ST);
-    for (int j = lane; j < S; j += 32)
-        dz[j] = make_float2(0.f, 0.f), sk[j] = make_float2(0.f, 0.f), stage[j] = 0.f;
+    float* dz = reinterpret_cast<float*>(wsm + Lay::DZ);
+    for (int j = lane; j < S; j += 32) dz[j] = 0.f;
     if (lane == 0) {
         mbar_init(bar0);
         mbar_init(bar0 + 8);
@@ -568,7 +576,7 @@ __global__ void __launch_bounds__(PB_NT) k_ppr_bulk(PprArgs A) {
                     float sum[C];
 #pragma unroll
                     for (int q = 0; q < C; ++q) sum[q] = __fsub_rn(acc.s[q], acc.c[q]);
-                    finish_row<C>(A, bC.v, rC, sum, lane, dz, sk, stage);
+                    finish_row<C>(A, bC.v, rC, sum, lane, dz);
                 }
             }
             // the half is refilled by the async proxy next: order our reads first
@@ -594,31 +602,16 @@ __global__ void __launch_bounds__(PB_NT) k_ppr_bulk(PprArgs A) {
         if (bC.valid && bC.cnt > 0) (void)mbar_wait(bar0 + 8 * hf, (parity >> hf) & 1u);
         if (bB.valid && bB.cnt > 0) (void)mbar_wait(bar0 + 8 * hB, (parity >> hB) & 1u);
     }
-    // the CTA's per-slot sums (warps in order, FP64) into its partial record
-    __syncthreads();
-    double* dst = A.part + (size_t)(A.part_base + blockIdx.x) * 2 * A.s_in;
-    for (uint32_t pos = threadIdx.x; pos < (uint32_t)S; pos += PB_NT) {
-        double a = 0.0, b = 0.0;
-        for (int w = 0; w < PB_WARPS; ++w) {
-            const unsigned char* o = pb_sm + w * Lay::WARP;
-            const float2 x = reinterpret_cast<const float2*>(o + Lay::DZ)[pos];
-            const float2 y = reinterpret_cast<const float2*>(o + Lay::SK)[pos];
-            a += (double)x.x - (double)x.y;
-            b += (double)y.x - (double)y.y;
-        }
-        const uint32_t j = Lanes<C>::slot(pos & 31, pos >> 5);
-        dst[j] = a;
-        dst[A.s_in + j] = b;
-    }
+    cta_fold<C>(A, reinterpret_cast<const float*>(pb_sm + Lay::DZ), PB_WARPS, Lay::WARP / 4);
 }
 
 // Sweep, part 2: every long row, its chunks' partials merged in chunk order,
 // then every seed row without in-edges.
 template <int C>
 __global__ void __launch_bounds__(PPR_NT) k_ppr_long(PprArgs A) {
-    extern __shared__ float2 ppr_sm[];
+    extern __shared__ float ppr_sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const WarpSmem m(ppr_sm, A.s_in, warp, lane);
+    float* dz = warp_dz(ppr_sm, A.s_in, warp, lane);
     const uint32_t gw = blockIdx.x * PPR_WARPS + warp, nw = gridDim.x * PPR_WARPS;
     for (uint32_t k = gw; k < A.n_long; k += nw) {
         const uint4 lr = A.longs[k];
@@ -636,7 +629,7 @@ __global__ void __launch_bounds__(PPR_NT) k_ppr_long(PprArgs A) {
         float sum[C];
 #pragma unroll
         for (int q = 0; q < C; ++q) sum[q] = t[q].value();
-        finish_row<C>(A, lr.x, r, sum, lane, m.dz, m.sk, m.stage);
+        finish_row<C>(A, lr.x, r, sum, lane, dz);
     }
     // seed rows without in-edges: an empty sum
     for (uint32_t k = gw; k < A.n_eseeds; k += nw) {
@@ -646,13 +639,60 @@ __global__ void __launch_bounds__(PPR_NT) k_ppr_long(PprArgs A) {
         float sum[C];
 #pragma unroll
         for (int q = 0; q < C; ++q) sum[q] = 0.f;
-        finish_row<C>(A, v, r, sum, lane, m.dz, m.sk, m.stage);
+        finish_row<C>(A, v, r, sum, lane, dz);
     }
-    cta_fold<C>(A, m);
+    cta_fold<C>(A, ppr_sm, PPR_WARPS, A.s_in);
 }
 
-// Sweep, part 3: out[j] = sum over the CTA partials of both kernels, in a
-// fixed order (a thread per value).
+// Sweep, part 3: the dangling mass of each output slot, the sum of zout over
+// the sink rows (zout of a sink holds its rank itself).  A sink without
+// in-edges and without a seed was skipped by the sweep and its row is zero,
+// so only sinks with an in-edge or a seed are read.  Warp gw takes the
+// 32-vertex groups gw, gw + warps, ... in vertex order, with compensation;
+// the CTA folds its warps in order (FP64) into the dangling-mass half of its
+// partial record.  C is the output width.
+template <int C>
+__global__ void __launch_bounds__(PPR_NT) k_ppr_sinks(PprArgs A, const uint32_t* __restrict__ pull_off) {
+    extern __shared__ float2 ps_sm[];
+    constexpr uint32_t S = 32 * C;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t gw = blockIdx.x * PPR_WARPS + warp, nw = gridDim.x * PPR_WARPS;
+    Kahan t[C];
+    for (uint32_t g = gw; (size_t)g * 32 < A.n; g += nw) {
+        const uint32_t v = g * 32 + lane;
+        bool take = false;
+        if (v < A.n)
+            take = A.dinv[v].x < 0.f &&
+                   (pull_off[v + 1] > pull_off[v] || A.seed_off[v + 1] > A.seed_off[v]);
+        uint32_t bits = __ballot_sync(0xffffffffu, take);
+        while (bits) {
+            const uint32_t b = (uint32_t)__ffs(bits) - 1;
+            bits &= bits - 1;
+            float x[C];
+            Lanes<C>::template load<true>(A.zout + (size_t)(g * 32 + b) * A.pitch, lane, x);
+#pragma unroll
+            for (int q = 0; q < C; ++q) t[q].add(x[q]);
+        }
+    }
+    float2* mine = ps_sm + (size_t)warp * S;
+#pragma unroll
+    for (int q = 0; q < C; ++q) mine[Lanes<C>::slot(lane, q)] = make_float2(t[q].s, t[q].c);
+    __syncthreads();
+    double* dst = A.part + (size_t)(A.part_base + blockIdx.x) * 2 * A.s_in;
+    for (uint32_t pos = threadIdx.x; pos < A.s_in; pos += PPR_NT) {
+        double b = 0.0;
+        if (pos < S)
+            for (int w = 0; w < PPR_WARPS; ++w) {
+                const float2 x = ps_sm[(size_t)w * S + pos];
+                b += (double)x.x + (double)x.y;
+            }
+        dst[pos] = 0.0;
+        dst[A.s_in + pos] = b;
+    }
+}
+
+// Sweep, part 4: out[j] = sum over the CTA partials of the three kernels, in
+// a fixed order (a thread per value).
 __global__ void k_ppr_fold(uint32_t n_values, uint32_t n_parts, const double* __restrict__ part,
                            double* __restrict__ out) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -922,7 +962,7 @@ PprLaunch ppr_shape(int variant, bool weighted) {
     if (variant == PPR_BULK) {
         auto* f = weighted ? k_ppr_bulk<C, true> : k_ppr_bulk<C, false>;
         L.threads1 = PB_NT;
-        L.smem1 = (size_t)PB_WARPS * PbLayout<C>::WARP;
+        L.smem1 = (size_t)PbLayout<C>::CTA;
         GTC_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem1));
         GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, PB_NT, L.smem1));
     } else {
@@ -956,6 +996,14 @@ void launch_ppr(PprArgs A, int variant, const PprLaunch& L1, unsigned grid2, cud
     GTC_LAUNCHED();
 }
 
+template <int C>
+void launch_sinks(PprArgs A, const uint32_t* pull_off, unsigned part_base, unsigned grid3,
+                  cudaStream_t s) {
+    A.part_base = part_base;
+    k_ppr_sinks<C><<<grid3, PPR_NT, (size_t)PPR_WARPS * 32 * C * sizeof(float2), s>>>(A, pull_off);
+    GTC_LAUNCHED();
+}
+
 void fold(const PprArgs& A, unsigned n_parts, double* out, cudaStream_t s) {
     const uint32_t nv = 2 * A.s_in;
     k_ppr_fold<<<(nv + 63) / 64, 64, 0, s>>>(nv, n_parts, A.part, out);
@@ -980,6 +1028,17 @@ void run_sweep(uint32_t C, const PprArgs& A, int variant, const PprLaunch& L1, u
     switch (C) {
 #define GTC_CASE(c) \
     case c: launch_ppr<c>(A, variant, L1, grid2, s); return;
+        GTC_PPR_C(GTC_CASE)
+#undef GTC_CASE
+    }
+    throw Error{GTC_ERR_CUDA, "batched personalised PageRank: bad slot count"};
+}
+
+void run_sinks(uint32_t c_out, const PprArgs& A, const uint32_t* pull_off, unsigned part_base,
+               unsigned grid3, cudaStream_t s) {
+    switch (c_out) {
+#define GTC_CASE(c) \
+    case c: launch_sinks<c>(A, pull_off, part_base, grid3, s); return;
         GTC_PPR_C(GTC_CASE)
 #undef GTC_CASE
     }
@@ -1144,7 +1203,11 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     const unsigned grid2 =
         std::max(1u, std::min((S.n_long + n_es + PPR_WARPS - 1) / PPR_WARPS, (unsigned)sms));
     DevBuf<float2> cpart((size_t)S.n_chunks * s_in, s);
-    DevBuf<double> part((size_t)(grid1_max + grid2) * 2 * s_in, s), out(2 * (size_t)s_in, s);
+    // the dangling-mass kernel: a warp per 32-vertex group, 2 CTAs per SM
+    const unsigned grid3 =
+        std::max(1u, std::min((unsigned)(((size_t)n + 32 * PPR_WARPS - 1) / (32 * PPR_WARPS)),
+                              2u * (unsigned)sms));
+    DevBuf<double> part((size_t)(grid1_max + grid2 + grid3) * 2 * s_in, s), out(2 * (size_t)s_in, s);
     DevBuf<uint32_t> dmap(2 * (size_t)s_in, s);  // col_in, then out_slot
     DevBuf<float> dps(s_in, s);
     DevBuf<uint2> dpairs(s_in, s);
@@ -1180,18 +1243,24 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     total.start();
     const uint32_t handoff = PPR_HANDOFF;
     while (running > 0) {
-        // the output layout: the columns still running, packed
+        // the output layout: the columns still running keep their slots while
+        // they need as many lines as now (a converged column leaves a hole),
+        // and are packed into the lowest slots when they need fewer
+        uint32_t active = 0;
+        for (uint32_t j = 0; j < s_in; ++j)
+            if (col_in[j] != PPR_NONE && !done[col_in[j]]) ++active;
+        const uint32_t c_out = ppr_lines(active);
+        const uint32_t s_out = 32 * c_out;
+        const bool in_place = c_out == C;
         out_slot.assign(s_in, PPR_NONE);
-        col_out.clear();
-        for (uint32_t j = 0; j < s_in; ++j) {
+        col_out.assign(s_out, PPR_NONE);
+        for (uint32_t j = 0, k = 0; j < s_in; ++j) {
             const uint32_t c = col_in[j];
             if (c == PPR_NONE || done[c]) continue;
-            out_slot[j] = (uint32_t)col_out.size();
-            col_out.push_back(c);
+            out_slot[j] = in_place ? j : k++;
+            col_out[out_slot[j]] = c;
         }
-        const uint32_t c_out = ppr_lines((uint32_t)col_out.size());
-        const uint32_t s_out = 32 * c_out;
-        col_out.resize(s_out, PPR_NONE);
+        A.in_place = in_place ? 1u : 0u;
         hps.assign(s_in, 0.f);
         for (uint32_t j = 0; j < s_in; ++j)
             if (col_in[j] != PPR_NONE) hps[j] = (float)psink_col[col_in[j]];
@@ -1206,10 +1275,11 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
         L1.grid1 = std::min(grid1_max, L1.grid1);
         if (in.timing) tsw.start();
         run_sweep(C, A, variant, L1, grid2, s);
-        fold(A, L1.grid1 + grid2, out.get(), s);
+        run_sinks(c_out, A, view.pull_off, L1.grid1 + grid2, grid3, s);
+        fold(A, L1.grid1 + grid2 + grid3, out.get(), s);
         if (in.timing) tsw.stop();
-        L += 3;
-        SL += 3;
+        L += 4;
+        SL += 4;
         hout.resize(2 * (size_t)s_in);
         GTC_CUDA(cudaMemcpyAsync(hout.data(), out.get(), 2 * (size_t)s_in * sizeof(double),
                                  cudaMemcpyDeviceToHost, s));
@@ -1225,7 +1295,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
             const uint32_t c = col_in[j];
             if (c == PPR_NONE || out_slot[j] == PPR_NONE) continue;
             in.iters[c] = sweeps;
-            psink_col[c] = hout[s_in + j];
+            psink_col[c] = hout[s_in + out_slot[j]];  // the mass is per output slot
             if (hout[j] < in.params.epsilon ||
                 (in.params.max_iter > 0 && sweeps == in.params.max_iter)) {
                 done[c] = 1;
