@@ -899,7 +899,7 @@ def main():
     opt_h = _ffi.Options(_ffi.GTC_PREC_F32, 0, C.c_void_p(stream.cuda_stream), 0, 0)
 
     def solve_host():
-        rank_np[:] = 1.0 / n  # the warm-start map the caller hands in
+        rank_host.fill_(1.0 / n)  # the warm-start map the caller hands in (ATen's threaded fill)
         res = _ffi.Result()
         _ffi.check(L.gtc_pagerank(h, None, _ffi.ptr(w_np, _ffi.f64p), 0 if w_np is None else m,
                                   None, 0, DAMPING, C.byref(e2e_params),
