@@ -200,6 +200,7 @@ __device__ __forceinline__ float gather(const SweepArgs& A, const float* hot, ui
 template <int MODE, bool WEIGHTED, int NT, bool HOT>
 __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
     constexpr int SP_WARPS = NT / 32;
+    constexpr bool ROUND8 = NT >= 1024;  // rounds of eight gathers a lane (see the slices)
     extern __shared__ float hot[];  // x[0 .. hot_n)
     using Acc = typename SweepAcc<MODE>::type;
     if (A.stop && *A.stop) return;  // the same for every CTA: before any barrier
@@ -269,7 +270,6 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
             // measured 1.3 % faster than four on RMAT-24 at the same 64
             // registers (fewer threads for more registers were slower); the
             // 256-thread kernel, at 40 registers, keeps rounds of four.
-            constexpr bool ROUND8 = NT >= 1024;
             RowIn rin;
             if (ROUND8 && len >= 8) {
                 uint32_t sv[8];
@@ -361,6 +361,24 @@ __global__ void __launch_bounds__(NT, HOT ? 1 : 6) k_sweep(SweepArgs A) {
                 kl.add(v2);
                 kl.add(v3);
             };
+            // (the 1024-thread kernels: rounds of eight, as in the slices)
+            if (ROUND8 && p + 224 < e) {
+                uint32_t sv[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) sv[k] = __ldcs(A.other + p + 32 * k);
+                for (; p + 256 + 224 < e; p += 256) {
+                    uint32_t nv[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) nv[k] = __ldcs(A.other + p + 256 + 32 * k);
+                    round(p, sv[0], sv[1], sv[2], sv[3]);
+                    round(p + 128, sv[4], sv[5], sv[6], sv[7]);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) sv[k] = nv[k];
+                }
+                round(p, sv[0], sv[1], sv[2], sv[3]);
+                round(p + 128, sv[4], sv[5], sv[6], sv[7]);
+                p += 256;
+            }
             if (p + 96 < e) {
                 uint32_t s0 = __ldcs(A.other + p), s1 = __ldcs(A.other + p + 32),
                          s2 = __ldcs(A.other + p + 64), s3 = __ldcs(A.other + p + 96);
