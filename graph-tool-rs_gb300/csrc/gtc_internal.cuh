@@ -158,6 +158,7 @@ struct PprSched {
     DevBuf<uint4> longs;    // {row, first chunk, chunks, 0}
     uint32_t n_items = 0, n_chunks = 0, n_long = 0;
     uint32_t n_empty = 0;  // single rows without pull entries (the last items)
+    uint32_t n_heavy = 0;  // chunks and single rows of at least 64 pull entries (the first items)
     bool built = false;
 };
 

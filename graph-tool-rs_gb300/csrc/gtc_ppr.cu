@@ -28,9 +28,15 @@
 // is dropped from the next sweep's output layout: the survivors are packed
 // into the lowest slots, so a sweep reads and writes ceil(active / 32) lines
 // per row, not B / 32.  The sweep that drops a column still gathers it (its
-// input layout is the previous sweep's output layout).  When at most
-// PPR_HANDOFF columns are left, each is finished by the single-vector solver
-// (gtc_centrality.cu) from its current iterate.
+// input layout is the previous sweep's output layout).
+//
+// Narrow rows.  With at most 16 columns left (8), the iterate is repacked
+// into rows of 16 (8) floats, two (one) 32-byte sectors a row, and a group of
+// 16 (8) lanes takes a work item, lane k summing column k (k_ppr_narrow):
+// one sector request per gathered row instead of a 128-byte line, and two
+// (four) rows per warp instruction.  When at most PPR_HANDOFF columns are
+// left, each is finished by the single-vector solver (gtc_centrality.cu) from
+// its current iterate.
 //
 // Schedule.  Rows with more than PPR_CHUNK in-edges are cut into chunks of
 // PPR_CHUNK entries; the first kernel of a sweep runs every chunk (a warp
@@ -72,10 +78,14 @@ constexpr int PPR_WARPS = PPR_NT / 32;
 constexpr uint32_t PPR_CHUNK = 1024;  // rows with more in-edges are cut into chunks
 constexpr uint32_t PPR_MAXB = 512;    // largest batch (16 lines per row)
 constexpr uint32_t PPR_NONE = 0xFFFFFFFFu;
+// At most this many columns left: narrow rows (k_ppr_narrow).
+constexpr uint32_t PPR_NARROW = 16;
 // At most this many columns left: each is finished by the single-vector
-// solver from its current iterate (a batched sweep of one line costs about
-// as much as this many single-vector sweeps).
-constexpr uint32_t PPR_HANDOFF = 8;
+// solver from its current iterate (a narrow sweep of 8 columns costs about
+// as much as three single-vector sweeps).
+constexpr uint32_t PPR_HANDOFF = 2;
+// Narrow rows: items of at least this many entries take a whole warp.
+constexpr uint32_t PPR_HEAVY = 64;
 
 struct PprArgs {
     uint32_t n, s_in, s_out;             // slots used per row of zin and zout
@@ -87,6 +97,7 @@ struct PprArgs {
     uint32_t n_long;
     const uint32_t* __restrict__ eseeds; // seed rows without in-edges
     uint32_t n_eseeds;
+    uint32_t n_heavy;                    // items of at least PPR_HEAVY entries (the first)
     const uint32_t* __restrict__ other;
     const float* __restrict__ w;         // pull-ordered weights or null
     const float* __restrict__ zin;       // [n][pitch], slots [0, s_in) used
@@ -644,6 +655,208 @@ __global__ void __launch_bounds__(PPR_NT) k_ppr_long(PprArgs A) {
     cta_fold<C>(A, ppr_sm, PPR_WARPS, A.s_in);
 }
 
+// ---------------------------------------------------------------------------
+// Narrow rows: Z is [n][K] (K = 8 or 16), slot k of every row is column
+// col_in[k] (PPR_NONE: no longer computed, stored as 0).  A group of K lanes
+// takes work items gg, gg + groups, ...; lane k of the group sums slot k.
+
+// What a row's update reads besides its sum, for lane k (loaded before the
+// gathers).
+struct NarrowIn {
+    float2 dd;
+    uint32_t sb, se;
+    float z;
+    __device__ __forceinline__ void load(const PprArgs& A, uint32_t v, uint32_t K, uint32_t k) {
+        dd = A.dinv[v];
+        sb = A.seed_off[v];
+        se = A.seed_off[v + 1];
+        z = A.zin[(size_t)v * K + k];
+    }
+};
+
+// The sources (and weights) of the pull entries [p0, min(p0 + K, e)) that
+// lane k of a group holds: entry p0 + k.
+template <bool W>
+struct NarrowIdx {
+    uint32_t src = 0;
+    float w = 1.f;
+    __device__ __forceinline__ void load(const PprArgs& A, uint32_t p0, uint32_t e, uint32_t k) {
+        if (p0 + k < e) {
+            src = __ldg(A.other + p0 + k);
+            if (W) w = __ldg(A.w + p0 + k);
+        }
+    }
+};
+
+// Compensated sum (Kahan, value s + c) of slot k of the zin rows over the
+// blocks of K pull entries starting at p0, p0 + step, ... below e: lane k
+// holds a block's K sources (the next block's are loaded before this one's
+// gathers) and the group shares them by shuffles; a block's gathers are all
+// in flight before they are added.
+template <int K, bool W>
+__device__ __forceinline__ Kahan narrow_sum(const PprArgs& A, uint32_t p0, uint32_t step,
+                                           uint32_t e, uint32_t k, uint32_t gmask) {
+    Kahan acc;
+    NarrowIdx<W> ix;
+    if (p0 < e) ix.load(A, p0, e, k);
+    for (; p0 < e; p0 += step) {
+        const uint32_t cnt = min((uint32_t)K, e - p0);
+        NarrowIdx<W> nx;
+        if (p0 + step < e) nx.load(A, p0 + step, e, k);
+        float v[K];
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+            const uint32_t src = __shfl_sync(gmask, ix.src, u, K);
+            v[u] = (uint32_t)u < cnt ? __ldg(A.zin + (size_t)src * K + k) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+            const float ww = W ? __shfl_sync(gmask, ix.w, u, K) : 1.f;
+            if ((uint32_t)u < cnt) acc.add(W ? __fmul_rn(v[u], ww) : v[u]);
+        }
+        ix = nx;
+    }
+    return acc;
+}
+
+// Row v's new value in slot k (the same arithmetic as finish_row), its
+// change and dangling mass into the lane's compensated partials.
+template <int K>
+__device__ __forceinline__ void narrow_finish(const PprArgs& A, uint32_t v, const NarrowIn& r,
+                                              float sum, uint32_t k, uint32_t os, uint32_t col,
+                                              float ps, Kahan& kd, Kahan& kk) {
+    float* zn = A.zout + (size_t)v * K + k;
+    if (os == PPR_NONE) {
+        *zn = 0.f;
+        return;
+    }
+    const bool snk = r.dd.x < 0.f;
+    const float prev = snk ? r.z : __fmul_rn(r.z, r.dd.x);
+    float nv;
+    if (r.se == r.sb) {
+        nv = __fmul_rn(A.d, sum);  // no seed: the general form with pv = 0, bit for bit
+    } else {
+        float pv = 0.f;
+        for (uint32_t t = r.sb; t < r.se; ++t) {
+            const uint2 sd = A.seeds[t];
+            if (sd.x == col) pv = __uint_as_float(sd.y);
+        }
+        const float x = __fadd_rn(__fmul_rn(ps, pv), sum);
+        nv = __fadd_rn(__fmul_rn(A.one_minus_d, pv), __fmul_rn(A.d, x));
+    }
+    kd.add(fabsf(__fsub_rn(nv, prev)));
+    if (snk) kk.add(nv);
+    *zn = snk ? nv : __fmul_rn(nv, r.dd.y);
+}
+
+// The CTA's per-slot change and dangling mass (lanes in thread order, FP64)
+// into its partial record.
+template <int K>
+__device__ __forceinline__ void narrow_fold(const PprArgs& A, Kahan kd, Kahan kk, float4* red) {
+    red[threadIdx.x] = make_float4(kd.s, kd.c, kk.s, kk.c);
+    __syncthreads();
+    double* dst = A.part + (size_t)(A.part_base + blockIdx.x) * 2 * K;
+    if (threadIdx.x < K) {
+        double a = 0.0, b = 0.0;
+        for (uint32_t t = threadIdx.x; t < blockDim.x; t += K) {
+            const float4 x = red[t];
+            a += (double)x.x + (double)x.y;
+            b += (double)x.z + (double)x.w;
+        }
+        dst[threadIdx.x] = a;
+        dst[K + threadIdx.x] = b;
+    }
+}
+
+// Narrow sweep, part 1: every long-row chunk (partials to cpart) and every
+// single row.  The first n_heavy items (chunks and rows of at least
+// PPR_HEAVY entries) take a warp each, its groups summing alternate blocks
+// of K entries and merged in group order; the others take a group each.
+template <int K, bool W>
+__global__ void __launch_bounds__(PPR_NT) k_ppr_narrow(PprArgs A) {
+    __shared__ float4 red[PPR_NT];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t k = lane % K, gl = lane / K;
+    const uint32_t gmask = K == 32 ? 0xffffffffu : ((1u << K) - 1u) << (gl * K);
+    constexpr uint32_t GPW = 32 / K;
+    const uint32_t gw = blockIdx.x * PPR_WARPS + warp, nw = gridDim.x * PPR_WARPS;
+    const uint32_t os = A.out_slot[k], col = A.col_in[k];
+    const float ps = A.psink[k];
+    Kahan kd, kk;
+    for (uint32_t it = gw; it < A.n_heavy; it += nw) {
+        const uint4 cur = A.items[it];
+        NarrowIn r;
+        if (it >= A.n_chunks) r.load(A, cur.x, K, k);
+        Kahan acc = narrow_sum<K, W>(A, cur.y + gl * K, GPW * K, cur.z, k, gmask);
+#pragma unroll
+        for (uint32_t g2 = 1; g2 < GPW; ++g2) {
+            const float os2 = __shfl_sync(0xffffffffu, acc.s, (int)(g2 * K + k));
+            const float oc2 = __shfl_sync(0xffffffffu, acc.c, (int)(g2 * K + k));
+            if (gl == 0) acc.merge(os2, oc2);
+        }
+        if (gl == 0) {
+            if (it < A.n_chunks)
+                A.cpart[(size_t)it * A.s_in + k] = make_float2(acc.s, acc.c);
+            else
+                narrow_finish<K>(A, cur.x, r, acc.value(), k, os, col, ps, kd, kk);
+        }
+    }
+    const uint32_t gg = gw * GPW + gl, ng = nw * GPW;
+    for (uint32_t it = A.n_heavy + gg; it < A.n_items; it += ng) {
+        const uint4 cur = A.items[it];
+        NarrowIn r;
+        r.load(A, cur.x, K, k);
+        const Kahan acc = narrow_sum<K, W>(A, cur.y, K, cur.z, k, gmask);
+        narrow_finish<K>(A, cur.x, r, acc.value(), k, os, col, ps, kd, kk);
+    }
+    narrow_fold<K>(A, kd, kk, red);
+}
+
+// Narrow sweep, part 2: every long row (its chunks' partials merged in chunk
+// order), then every seed row without in-edges.
+template <int K>
+__global__ void __launch_bounds__(PPR_NT) k_ppr_narrow_long(PprArgs A) {
+    __shared__ float4 red[PPR_NT];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t k = lane % K, gl = lane / K;
+    constexpr uint32_t GPW = 32 / K;
+    const uint32_t gg = (blockIdx.x * PPR_WARPS + warp) * GPW + gl;
+    const uint32_t ng = gridDim.x * PPR_WARPS * GPW;
+    const uint32_t os = A.out_slot[k], col = A.col_in[k];
+    const float ps = A.psink[k];
+    Kahan kd, kk;
+    for (uint32_t i = gg; i < A.n_long; i += ng) {
+        const uint4 lr = A.longs[i];
+        NarrowIn r;
+        r.load(A, lr.x, K, k);
+        Kahan t;
+        for (uint32_t c = lr.y; c < lr.y + lr.z; ++c) {
+            const float2 pq = __ldcg(A.cpart + (size_t)c * A.s_in + k);
+            t.merge(pq.x, pq.y);
+        }
+        narrow_finish<K>(A, lr.x, r, t.value(), k, os, col, ps, kd, kk);
+    }
+    for (uint32_t i = gg; i < A.n_eseeds; i += ng) {
+        const uint32_t v = A.eseeds[i];
+        NarrowIn r;
+        r.load(A, v, K, k);
+        narrow_finish<K>(A, v, r, 0.f, k, os, col, ps, kd, kk);
+    }
+    narrow_fold<K>(A, kd, kk, red);
+}
+
+// zdst[v][k] = zsrc[v][slot[k]] (0 where slot[k] is PPR_NONE): the running
+// columns into narrow rows.
+__global__ void k_ppr_narrow_pack(uint32_t n, uint32_t K, uint32_t src_pitch,
+                                  const uint32_t* __restrict__ slot, const float* __restrict__ zsrc,
+                                  float* __restrict__ zdst) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)n * K) return;
+    const uint32_t v = (uint32_t)(i / K), k = (uint32_t)(i % K);
+    const uint32_t j = slot[k];
+    zdst[i] = j == PPR_NONE ? 0.f : zsrc[(size_t)v * src_pitch + j];
+}
+
 // Sweep, part 3: the dangling mass of each output slot, the sum of zout over
 // the sink rows (zout of a sink holds its rank itself).  A sink without
 // in-edges and without a seed was skipped by the sweep and its row is zero,
@@ -827,7 +1040,8 @@ __global__ void k_gather_w_ppr(uint32_t m, const uint32_t* __restrict__ eid,
 }
 
 // schedule keys: 0 for a row cut into chunks, else PPR_CHUNK + 1 - in-degree
-// (cnt[0]: rows cut into chunks, cnt[1]: rows without pull entries)
+// (cnt[0]: rows cut into chunks, cnt[1]: rows without pull entries, cnt[2]:
+// single rows of at least PPR_HEAVY entries)
 __global__ void k_ppr_keys(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ key,
                            unsigned* __restrict__ cnt) {
     const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -836,6 +1050,7 @@ __global__ void k_ppr_keys(uint32_t n, const uint32_t* __restrict__ off, uint32_
     key[v] = dg > PPR_CHUNK ? 0u : PPR_CHUNK + 1 - dg;
     if (dg > PPR_CHUNK) atomicAdd(cnt, 1u);
     if (dg == 0) atomicAdd(cnt + 1, 1u);
+    if (dg >= PPR_HEAVY && dg <= PPR_CHUNK) atomicAdd(cnt + 2, 1u);
 }
 
 __global__ void k_ppr_row_items(uint32_t k, const uint32_t* __restrict__ pos,
@@ -855,16 +1070,16 @@ void build_ppr_schedule(gtc_graph* g, const View& view, cudaStream_t s, PprSched
     GTC_CUDA(cudaStreamSynchronize(s));
     uint64_t L = 0;
     DevBuf<uint32_t> key(n, h), skey(n, h), pos(n, h);
-    DevBuf<unsigned> cnt(2, h);
-    GTC_CUDA(cudaMemsetAsync(cnt.get(), 0, 2 * sizeof(unsigned), h));
+    DevBuf<unsigned> cnt(3, h);
+    GTC_CUDA(cudaMemsetAsync(cnt.get(), 0, 3 * sizeof(unsigned), h));
     if (n) {
         k_ppr_keys<<<grid_for(n, 256, 1u << 30), 256, 0, h>>>(n, view.pull_off, key.get(), cnt.get());
         GTC_LAUNCHED();
         L++;
         sort_positions_by_key(key.get(), n, PPR_CHUNK + 2, skey.get(), pos.get(), h, &L);
     }
-    unsigned cnts[2] = {0, 0};
-    GTC_CUDA(cudaMemcpyAsync(cnts, cnt.get(), 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, h));
+    unsigned cnts[3] = {0, 0, 0};
+    GTC_CUDA(cudaMemcpyAsync(cnts, cnt.get(), 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, h));
     GTC_CUDA(cudaStreamSynchronize(h));
     const unsigned n_long = cnts[0];
     std::vector<uint4> lrec(n_long);
@@ -891,6 +1106,7 @@ void build_ppr_schedule(gtc_graph* g, const View& view, cudaStream_t s, PprSched
     S.n_chunks = (uint32_t)chunks.size();
     S.n_items = S.n_chunks + n_single;
     S.n_empty = cnts[1];  // the last single rows (the highest key)
+    S.n_heavy = S.n_chunks + cnts[2];  // chunks, then the single rows of the lowest keys
     S.items.alloc(S.n_items, h);
     S.longs.alloc(S.n_long, h);
     if (S.n_chunks)
@@ -1043,6 +1259,31 @@ void run_sinks(uint32_t c_out, const PprArgs& A, const uint32_t* pull_off, unsig
 #undef GTC_CASE
     }
     throw Error{GTC_ERR_CUDA, "batched personalised PageRank: bad slot count"};
+}
+
+template <int K>
+void launch_narrow(PprArgs A, bool weighted, unsigned grid1, unsigned grid2, cudaStream_t s) {
+    A.part_base = 0;
+    if (weighted)
+        k_ppr_narrow<K, true><<<grid1, PPR_NT, 0, s>>>(A);
+    else
+        k_ppr_narrow<K, false><<<grid1, PPR_NT, 0, s>>>(A);
+    GTC_LAUNCHED();
+    A.part_base = grid1;
+    k_ppr_narrow_long<K><<<grid2, PPR_NT, 0, s>>>(A);
+    GTC_LAUNCHED();
+}
+
+// CTAs of the narrow part 1: as many as fit on every SM at once.
+unsigned narrow_grid(uint32_t K, bool weighted, int sms) {
+    int per_sm = 0;
+    if (K == 8)
+        GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, weighted ? k_ppr_narrow<8, true> : k_ppr_narrow<8, false>, PPR_NT, 0));
+    else
+        GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, weighted ? k_ppr_narrow<16, true> : k_ppr_narrow<16, false>, PPR_NT, 0));
+    return (unsigned)std::max(1, per_sm * sms);
 }
 
 // Lines per row for `active` columns: ceil(active / 32), rounded up to 6 or
@@ -1221,6 +1462,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     A.items = S.items.get(), A.n_items = S.n_items - S.n_empty, A.n_chunks = S.n_chunks;
     A.longs = S.longs.get(), A.n_long = S.n_long;
     A.eseeds = des.get(), A.n_eseeds = n_es;
+    A.n_heavy = S.n_heavy;
     A.other = view.pull_other, A.w = wpull.get();
     A.dinv = dinv.get();
     A.seed_off = dso.get(), A.seeds = dsd.get();
@@ -1241,8 +1483,154 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
     float *zc = z0.get(), *zx = z1.get();
     PprTimer total(s), tsw(s);
     total.start();
-    const uint32_t handoff = PPR_HANDOFF;
+    uint32_t K = 0;  // narrow row width, 0 while the rows are lines
+    uint32_t pitch = P;
+    const bool W = A.w != nullptr;
+    unsigned grid_n = 0;
     while (running > 0) {
+        uint32_t running_slots = 0;
+        for (uint32_t j = 0; j < s_in; ++j)
+            if (col_in[j] != PPR_NONE && !done[col_in[j]]) ++running_slots;
+        const uint32_t want = running_slots <= 8 ? 8u : running_slots <= PPR_NARROW ? 16u : 0u;
+        if (want && want != K && n) {
+            // the running columns, in slot order, into rows of `want` floats;
+            // the other buffer's rows of that width start at zero (the rows
+            // without in-edges are never written)
+            std::vector<uint32_t> src_slot(want, PPR_NONE), ncol(want, PPR_NONE);
+            for (uint32_t j = 0, k = 0; j < s_in; ++j) {
+                const uint32_t c = col_in[j];
+                if (c == PPR_NONE || done[c]) continue;
+                src_slot[k] = j;
+                ncol[k++] = c;
+            }
+            GTC_CUDA(cudaMemcpyAsync(dmap.get(), src_slot.data(), want * 4, cudaMemcpyHostToDevice, s));
+            k_ppr_narrow_pack<<<grid_for((size_t)n * want, TB, 1u << 30), TB, 0, s>>>(
+                n, want, pitch, dmap.get(), zc, zx);
+            GTC_LAUNCHED();
+            L++;
+            GTC_CUDA(cudaMemsetAsync(zc, 0, (size_t)n * want * sizeof(float), s));
+            std::swap(zc, zx);
+            col_in = ncol;
+            s_in = want;
+            K = want;
+            pitch = want;
+            grid_n = std::min(grid1_max, narrow_grid(K, W, sms));
+        }
+        if (K) {
+            // a narrow sweep: every running column keeps its slot
+            out_slot.assign(K, PPR_NONE);
+            hps.assign(K, 0.f);
+            for (uint32_t k = 0; k < K; ++k) {
+                const uint32_t c = col_in[k];
+                if (c == PPR_NONE) continue;
+                hps[k] = (float)psink_col[c];
+                if (!done[c]) out_slot[k] = k;
+            }
+            maps.assign(col_in.begin(), col_in.end());
+            maps.insert(maps.end(), out_slot.begin(), out_slot.end());
+            GTC_CUDA(cudaMemcpyAsync(dmap.get(), maps.data(), maps.size() * 4, cudaMemcpyHostToDevice, s));
+            GTC_CUDA(cudaMemcpyAsync(dps.get(), hps.data(), K * sizeof(float), cudaMemcpyHostToDevice, s));
+            A.col_in = dmap.get(), A.out_slot = dmap.get() + K;
+            A.s_in = A.s_out = K;
+            A.pitch = K;
+            A.in_place = 1u;
+            A.zin = zc, A.zout = zx;
+            if (in.timing) tsw.start();
+            if (K == 8)
+                launch_narrow<8>(A, W, grid_n, grid2, s);
+            else
+                launch_narrow<16>(A, W, grid_n, grid2, s);
+            fold(A, grid_n + grid2, out.get(), s);
+            if (in.timing) tsw.stop();
+            L += 3;
+            SL += 3;
+            hout.resize(2 * (size_t)K);
+            GTC_CUDA(cudaMemcpyAsync(hout.data(), out.get(), 2 * (size_t)K * sizeof(double),
+                                     cudaMemcpyDeviceToHost, s));
+            int herr = 0;
+            GTC_CUDA(cudaMemcpyAsync(&herr, derr.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+            GTC_CUDA(cudaStreamSynchronize(s));
+            GTC_REQUIRE(herr == 0, GTC_ERR_CUDA,
+                        "batched personalised PageRank: a gathered row did not arrive in time");
+            if (in.timing) sweep_ms += tsw.ms();
+            ++sweeps;
+            store.clear();
+            for (uint32_t k = 0; k < K; ++k) {
+                const uint32_t c = col_in[k];
+                if (c == PPR_NONE || out_slot[k] == PPR_NONE) continue;
+                in.iters[c] = sweeps;
+                psink_col[c] = hout[K + k];
+                if (hout[k] < in.params.epsilon ||
+                    (in.params.max_iter > 0 && sweeps == in.params.max_iter)) {
+                    done[c] = 1;
+                    --running;
+                    store.push_back(make_uint2(k, c));
+                }
+            }
+            if (!store.empty()) {
+                const uint32_t nk = (uint32_t)store.size();
+                GTC_CUDA(cudaMemcpyAsync(dpairs.get(), store.data(), nk * sizeof(uint2),
+                                         cudaMemcpyHostToDevice, s));
+                dim3 g2((n + 31) / 32, (nk + 31) / 32), blk(32, 8);
+                k_ppr_store<<<g2, blk, 0, s>>>(n, K, nk, dpairs.get(), g->iperm.get(), dinv.get(),
+                                              zx, in.out, in.out_dtype);
+                GTC_LAUNCHED();
+                L++;
+            }
+            std::swap(zc, zx);
+            if (running > 0 && running <= PPR_HANDOFF) {
+                // the last columns: their iterates to the output, then the
+                // single-vector solver continues each from there (pagerank_with
+                // from a warm start is the same iteration)
+                const size_t esz = in.out_dtype == GTC_F64 ? 8 : 4;
+                DevBuf<float> pers(n, s), dvals(64, s);
+                DevBuf<uint32_t> dverts(64, s);
+                for (uint32_t k = 0; k < K; ++k) {
+                    const uint32_t c = col_in[k];
+                    if (c == PPR_NONE || done[c]) continue;
+                    const uint2 pair = make_uint2(k, c);
+                    GTC_CUDA(cudaMemcpyAsync(dpairs.get(), &pair, sizeof(uint2), cudaMemcpyHostToDevice, s));
+                    dim3 g2((n + 31) / 32, 1), blk(32, 8);
+                    k_ppr_store<<<g2, blk, 0, s>>>(n, K, 1, dpairs.get(), g->iperm.get(), dinv.get(),
+                                                  zc, in.out, in.out_dtype);
+                    GTC_LAUNCHED();
+                    const uint64_t sb = in.seed_off[c], se = in.seed_off[c + 1];
+                    std::vector<uint32_t> hv;
+                    std::vector<float> hval;
+                    for (uint64_t t = sb; t < se; ++t) {
+                        hv.push_back(in.seed_vertices[t]);
+                        hval.push_back((float)(in.seed_values ? in.seed_values[t] : 1.0 / (double)(se - sb)));
+                    }
+                    if (hv.size() > dverts.n) dverts.alloc(hv.size(), s), dvals.alloc(hv.size(), s);
+                    GTC_CUDA(cudaMemsetAsync(pers.get(), 0, (size_t)n * sizeof(float), s));
+                    if (!hv.empty()) {
+                        GTC_CUDA(cudaMemcpyAsync(dverts.get(), hv.data(), hv.size() * 4, cudaMemcpyHostToDevice, s));
+                        GTC_CUDA(cudaMemcpyAsync(dvals.get(), hval.data(), hval.size() * 4, cudaMemcpyHostToDevice, s));
+                        k_ppr_pers<<<1, 32, 0, s>>>((uint32_t)hv.size(), dverts.get(), dvals.get(), pers.get());
+                        GTC_LAUNCHED();
+                    }
+                    L += 2;
+                    SolveIn si{};
+                    si.weight = in.weight;
+                    si.pers.p = pers.get(), si.pers.len = n, si.pers.dtype = GTC_F32;
+                    si.damping = in.damping;
+                    si.params = in.params;
+                    si.params.max_iter = in.params.max_iter > 0 ? in.params.max_iter - sweeps : 0;
+                    si.x = static_cast<char*>(in.out) + (size_t)c * n * esz;
+                    si.x_dtype = in.out_dtype;
+                    si.had = n;
+                    si.precision = GTC_PREC_F32;
+                    gtc_result r{};
+                    pagerank(g, vw, si, &r, s);
+                    in.iters[c] = sweeps + r.iterations;
+                    L_solver += r.launches;  // already counted on the handle by the solver
+                    SL += r.sweep_launches;
+                    done[c] = 1;
+                }
+                running = 0;
+            }
+            continue;
+        }
         // the output layout: the columns still running keep their slots while
         // they need as many lines as now (a converged column leaves a hole),
         // and are packed into the lowest slots when they need fewer
@@ -1270,6 +1658,7 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
         GTC_CUDA(cudaMemcpyAsync(dps.get(), hps.data(), s_in * sizeof(float), cudaMemcpyHostToDevice, s));
         A.col_in = dmap.get(), A.out_slot = dmap.get() + s_in;
         A.s_in = s_in, A.s_out = s_out;
+        A.pitch = P;
         A.zin = zc, A.zout = zx;
         PprLaunch L1 = shape(C, variant, A.w != nullptr);
         L1.grid1 = std::min(grid1_max, L1.grid1);
@@ -1306,11 +1695,11 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
         // converged columns go to the output now, from this sweep's iterate
         // (a copy from pageable memory returns once the source is staged)
         if (!store.empty() && n) {
-            const uint32_t K = (uint32_t)store.size();
-            GTC_CUDA(cudaMemcpyAsync(dpairs.get(), store.data(), K * sizeof(uint2),
+            const uint32_t nk = (uint32_t)store.size();
+            GTC_CUDA(cudaMemcpyAsync(dpairs.get(), store.data(), nk * sizeof(uint2),
                                      cudaMemcpyHostToDevice, s));
-            dim3 g2((n + 31) / 32, (K + 31) / 32), blk(32, 8);
-            k_ppr_store<<<g2, blk, 0, s>>>(n, P, K, dpairs.get(), g->iperm.get(), dinv.get(), zx,
+            dim3 g2((n + 31) / 32, (nk + 31) / 32), blk(32, 8);
+            k_ppr_store<<<g2, blk, 0, s>>>(n, P, nk, dpairs.get(), g->iperm.get(), dinv.get(), zx,
                                           in.out, in.out_dtype);
             GTC_LAUNCHED();
             L++;
@@ -1319,57 +1708,6 @@ void ppr_batch(gtc_graph* g, const gtc_view* vw, const PprIn& in, gtc_result* re
         s_in = s_out;
         C = c_out;
         std::swap(zc, zx);
-        if (running > 0 && running <= handoff && n) {
-            // the last few columns: their iterates to the output, then the
-            // single-vector solver continues each from there (pagerank_with
-            // from a warm start is the same iteration)
-            const size_t esz = in.out_dtype == GTC_F64 ? 8 : 4;
-            DevBuf<float> pers(n, s), dvals(64, s);
-            DevBuf<uint32_t> dverts(64, s);
-            for (uint32_t j = 0; j < s_in; ++j) {
-                const uint32_t c = col_in[j];
-                if (c == PPR_NONE || done[c]) continue;
-                const uint2 pair = make_uint2(j, c);
-                GTC_CUDA(cudaMemcpyAsync(dpairs.get(), &pair, sizeof(uint2), cudaMemcpyHostToDevice, s));
-                dim3 g2((n + 31) / 32, 1), blk(32, 8);
-                k_ppr_store<<<g2, blk, 0, s>>>(n, P, 1, dpairs.get(), g->iperm.get(), dinv.get(),
-                                              zc, in.out, in.out_dtype);
-                GTC_LAUNCHED();
-                const uint64_t sb = in.seed_off[c], se = in.seed_off[c + 1];
-                std::vector<uint32_t> hv;
-                std::vector<float> hval;
-                for (uint64_t k = sb; k < se; ++k) {
-                    hv.push_back(in.seed_vertices[k]);
-                    hval.push_back((float)(in.seed_values ? in.seed_values[k] : 1.0 / (double)(se - sb)));
-                }
-                if (hv.size() > dverts.n) dverts.alloc(hv.size(), s), dvals.alloc(hv.size(), s);
-                GTC_CUDA(cudaMemsetAsync(pers.get(), 0, (size_t)n * sizeof(float), s));
-                if (!hv.empty()) {
-                    GTC_CUDA(cudaMemcpyAsync(dverts.get(), hv.data(), hv.size() * 4, cudaMemcpyHostToDevice, s));
-                    GTC_CUDA(cudaMemcpyAsync(dvals.get(), hval.data(), hval.size() * 4, cudaMemcpyHostToDevice, s));
-                    k_ppr_pers<<<1, 32, 0, s>>>((uint32_t)hv.size(), dverts.get(), dvals.get(), pers.get());
-                    GTC_LAUNCHED();
-                }
-                L += 2;
-                SolveIn si{};
-                si.weight = in.weight;
-                si.pers.p = pers.get(), si.pers.len = n, si.pers.dtype = GTC_F32;
-                si.damping = in.damping;
-                si.params = in.params;
-                si.params.max_iter = in.params.max_iter > 0 ? in.params.max_iter - sweeps : 0;
-                si.x = static_cast<char*>(in.out) + (size_t)c * n * esz;
-                si.x_dtype = in.out_dtype;
-                si.had = n;
-                si.precision = GTC_PREC_F32;
-                gtc_result r{};
-                pagerank(g, vw, si, &r, s);
-                in.iters[c] = sweeps + r.iterations;
-                L_solver += r.launches;  // already counted on the handle by the solver
-                SL += r.sweep_launches;
-                done[c] = 1;
-            }
-            running = 0;
-        }
     }
     total.stop();
     res->device_ms = total.ms();

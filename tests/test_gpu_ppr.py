@@ -98,9 +98,20 @@ def test_ppr_batch_seeds_without_in_edges(oracle, gtc, variant):
     _check(oracle, gtc, n, src, tgt, len(sets), gather=variant, sets=sets)
 
 
+@pytest.mark.parametrize("B", [5, 12])
+def test_ppr_batch_narrow_rows_from_the_start(oracle, gtc, B):
+    # at most 16 columns: rows of 8 or 16 floats from the first sweep, a
+    # group of lanes per row; weighted and reversed as well
+    from graph_tool import synth
+    n, src, tgt = synth.rmat_cpu(11, edge_factor=8, seed=12)
+    w = np.random.default_rng(4).uniform(0.1, 1.0, src.size)
+    _check(oracle, gtc, n, src, tgt, B, seed=13)
+    _check(oracle, gtc, n, src, tgt, B, weight=w, reversed=True, seed=14)
+
+
 def test_ppr_batch_max_iter_caps_every_column(oracle, gtc, variant):
     # a cap below convergence: every column stops at the cap with the
-    # iterate of that sweep (also through the single-vector hand-off)
+    # iterate of that sweep (also in the narrow rows of the last columns)
     from graph_tool import synth
     n, src, tgt, _ = synth.erdos_renyi_sinks(n=2000, m=16000)
     rng = np.random.default_rng(9)
