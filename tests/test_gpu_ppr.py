@@ -98,6 +98,13 @@ def test_ppr_batch_seeds_without_in_edges(oracle, gtc, variant):
     _check(oracle, gtc, n, src, tgt, len(sets), gather=variant, sets=sets)
 
 
+def test_ppr_batch_widest(oracle, gtc, variant):
+    # 512 columns: rows of 16 lines, then 12, 8, 6, 4 ... as columns converge
+    from graph_tool import synth
+    n, src, tgt, _ = synth.erdos_renyi_sinks(n=1500, m=12000)
+    _check(oracle, gtc, n, src, tgt, 512, seed=21, gather=variant)
+
+
 @pytest.mark.parametrize("B", [5, 12])
 def test_ppr_batch_narrow_rows_from_the_start(oracle, gtc, B):
     # at most 16 columns: rows of 8 or 16 floats from the first sweep, a
