@@ -98,6 +98,19 @@ def test_ppr_batch_seeds_without_in_edges(oracle, gtc, variant):
     _check(oracle, gtc, n, src, tgt, len(sets), gather=variant, sets=sets)
 
 
+def test_ppr_batch_zero_weights_make_sinks(oracle, gtc, variant):
+    # a vertex whose out-edges all weigh 0 is a sink by weight although its
+    # row is gathered (with weight 0); wide rows and narrow rows
+    from graph_tool import synth
+    n, src, tgt = synth.rmat_cpu(10, edge_factor=8, seed=17)
+    w = np.random.default_rng(5).uniform(0.1, 1.0, src.size)
+    zero_src = np.random.default_rng(6).choice(n, n // 10, replace=False)
+    w[np.isin(src, zero_src)] = 0.0
+    w[np.random.default_rng(7).random(src.size) < 0.05] = 0.0
+    _check(oracle, gtc, n, src, tgt, 40, weight=w, seed=18, gather=variant)
+    _check(oracle, gtc, n, src, tgt, 6, weight=w, seed=19, gather=variant)
+
+
 def test_ppr_batch_widest(oracle, gtc, variant):
     # 512 columns: rows of 16 lines, then 12, 8, 6, 4 ... as columns converge
     from graph_tool import synth
