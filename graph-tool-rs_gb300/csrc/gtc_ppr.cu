@@ -785,7 +785,7 @@ __global__ void __launch_bounds__(PPR_NT) k_ppr_narrow(PprArgs A) {
     Kahan kd, kk;
     for (uint32_t it = gw; it < A.n_heavy; it += nw) {
         const uint4 cur = A.items[it];
-        NarrowIn r;
+        NarrowIn r{};
         if (it >= A.n_chunks) r.load(A, cur.x, K, k);
         Kahan acc = narrow_sum<K, W>(A, cur.y + gl * K, GPW * K, cur.z, k, gmask);
 #pragma unroll
