@@ -25,10 +25,12 @@
 // Active columns only.  Columns converge at very different sweeps (for an
 // R-MAT graph and seed sets of 1-64 vertices the last column takes ~2.5x the
 // mean).  A column that converged is written to the output right away and
-// is dropped from the next sweep's output layout: the survivors are packed
-// into the lowest slots, so a sweep reads and writes ceil(active / 32) lines
-// per row, not B / 32.  The sweep that drops a column still gathers it (its
-// input layout is the previous sweep's output layout).
+// is no longer computed: the survivors keep their slots (a converged
+// column's slot becomes a hole, written as 0) until they fit in fewer lines,
+// then they are packed into the lowest slots, so a sweep reads and writes
+// about ceil(active / 32) lines per row, not B / 32.  The sweep that drops a
+// column still gathers it (its input layout is the previous sweep's output
+// layout).
 //
 // Narrow rows.  With at most 16 columns left (8), the iterate is repacked
 // into rows of 16 (8) floats, two (one) 32-byte sectors a row, and a group of
@@ -59,7 +61,7 @@
 // folded over warps and CTAs in FP64; shared memory goes to the gather rings
 // instead (see pb_rows).  The dangling mass per column is summed with Kahan
 // compensation per warp from the new iterate's sink rows and folded in FP64.
-// The per-row work stays off
+// In narrow rows both are compensated per lane.  The per-row work stays off
 // the FP64 pipe (on this GPU a few FP64 operations per row cost more than the
 // row's gathers): degrees and their inverses are precomputed in FP32.
 #include <algorithm>
