@@ -126,9 +126,13 @@ def measured_peaks():
 
 
 class Clocks:
-    """nvidia-smi samples during the timed region."""
+    """nvidia-smi samples (every 50 ms) kept if taken inside the timed region.
 
-    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+    The sampler starts before the warm-up, so that it is running when the
+    timed region starts; ``start()`` and ``stop()`` mark the region by wall
+    clock, and only the samples stamped inside it are summarised."""
+
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
@@ -136,12 +140,19 @@ class Clocks:
         self.idx = gpu_index
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
+
+    def start(self):
+        self.t0 = time.time()
+
+    def stop(self):
+        self.t1 = time.time()
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -161,19 +172,30 @@ class Clocks:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
+    @staticmethod
+    def _stamp(text):
+        import datetime
+        try:
+            return datetime.datetime.strptime(text, "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
+
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
-            if len(f) < 7:
+            if len(f) < 8:
                 continue
+            t = self._stamp(f[0])
+            if self.t0 is not None and (t is None or t < self.t0 or t > self.t1):
+                continue  # outside the timed region
             try:
-                sm.append(float(f[0]))
-                mx = float(f[1])
+                sm.append(float(f[1]))
+                mx = float(f[2])
             except ValueError:
                 continue
-            for nm, v in zip(names, f[3:7]):
+            for nm, v in zip(names, f[4:8]):
                 if v.lower() == "active":
                     reasons.add(nm)
         if not sm:
@@ -865,15 +887,16 @@ def main():
                                          C.byref(opt), C.byref(res)))
         return res
 
-    for _ in range(args.warmup):
-        solve_device()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     sweeps = sweep_ms = launches = sweep_launches = 0
     with Clocks(local) as clk:
+        for _ in range(args.warmup):
+            solve_device()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        clk.start()
         e0.record(stream)
         for _ in range(args.steps):
             r = solve_device()
@@ -883,6 +906,7 @@ def main():
             sweep_launches += r.sweep_launches
         e1.record(stream)
         torch.cuda.synchronize()
+        clk.stop()
     t_ms = max_over_ranks(e0.elapsed_time(e1), world)
     value = whole_job_gteps(world, m, sweeps, t_ms)
     iters_per_solve = sweeps / args.steps
