@@ -279,7 +279,8 @@ struct RowIn {
 // afterwards (k_ppr_sinks).  Nothing here runs on the FP64 pipe.
 template <int C>
 __device__ __forceinline__ void finish_row(const PprArgs& A, uint32_t v, const RowIn<C>& r,
-                                           const float (&sum)[C], int lane, float* dz) {
+                                           const float (&sum)[C], int lane, float* dz,
+                                           uint32_t amask) {
     const bool snk = r.dd.x < 0.f;
     const bool seeded = r.se > r.sb;
     uint32_t osv[C];
@@ -287,10 +288,13 @@ __device__ __forceinline__ void finish_row(const PprArgs& A, uint32_t v, const R
 #pragma unroll
     for (int q = 0; q < C; ++q) {
         const uint32_t j = Lanes<C>::slot(lane, q);
-        const uint32_t os = __ldg(A.out_slot + j);
-        osv[q] = os;
         outv[q] = 0.f;
-        if (os == PPR_NONE) continue;
+        if (!((amask >> q) & 1u)) {
+            osv[q] = PPR_NONE;
+            continue;
+        }
+        // in place the output slot is the input slot
+        osv[q] = A.in_place ? j : __ldg(A.out_slot + j);
         const float prev = snk ? r.z[q] : __fmul_rn(r.z[q], r.dd.x);
         float nv;
         if (!seeded) {
@@ -336,6 +340,17 @@ __device__ __forceinline__ void finish_row(const PprArgs& A, uint32_t v, const R
     }
 }
 
+// Bit q: the lane's q-th input slot is computed this sweep (out_slot is not
+// PPR_NONE), read once per kernel.
+template <int C>
+__device__ __forceinline__ uint32_t active_mask(const PprArgs& A, int lane) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int q = 0; q < C; ++q)
+        if (__ldg(A.out_slot + Lanes<C>::slot(lane, q)) != PPR_NONE) m |= 1u << q;
+    return m;
+}
+
 // Shared memory of the register-gather and long-row kernels: per warp [s_in]
 // partial L1 changes.
 inline size_t ppr_smem(uint32_t s_in) { return (size_t)PPR_WARPS * s_in * sizeof(float); }
@@ -371,6 +386,7 @@ __global__ void __launch_bounds__(PPR_NT) k_ppr_rows(PprArgs A) {
     extern __shared__ float ppr_sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float* dz = warp_dz(ppr_sm, A.s_in, warp, lane);
+    const uint32_t amask = active_mask<C>(A, lane);
     const uint32_t gw = blockIdx.x * PPR_WARPS + warp, nw = gridDim.x * PPR_WARPS;
     uint4 nxt = gw < A.n_items ? A.items[gw] : make_uint4(0u, 0u, 0u, 0u);
     for (uint32_t it = gw; it < A.n_items; it += nw) {
@@ -391,7 +407,7 @@ __global__ void __launch_bounds__(PPR_NT) k_ppr_rows(PprArgs A) {
             float sum[C];
 #pragma unroll
             for (int q = 0; q < C; ++q) sum[q] = __fsub_rn(acc.s[q], acc.c[q]);
-            finish_row<C>(A, cur.x, r, sum, lane, dz);
+            finish_row<C>(A, cur.x, r, sum, lane, dz, amask);
         }
     }
     cta_fold<C>(A, ppr_sm, PPR_WARPS, A.s_in);
@@ -488,6 +504,7 @@ __global__ void __launch_bounds__(PB_NT) k_ppr_bulk(PprArgs A) {
     const uint32_t bar0 = smem_u32(wsm + Lay::RING);
     float* dz = reinterpret_cast<float*>(wsm + Lay::DZ);
     for (int j = lane; j < S; j += 32) dz[j] = 0.f;
+    const uint32_t amask = active_mask<C>(A, lane);
     if (lane == 0) {
         mbar_init(bar0);
         mbar_init(bar0 + 8);
@@ -589,7 +606,7 @@ __global__ void __launch_bounds__(PB_NT) k_ppr_bulk(PprArgs A) {
                     float sum[C];
 #pragma unroll
                     for (int q = 0; q < C; ++q) sum[q] = __fsub_rn(acc.s[q], acc.c[q]);
-                    finish_row<C>(A, bC.v, rC, sum, lane, dz);
+                    finish_row<C>(A, bC.v, rC, sum, lane, dz, amask);
                 }
             }
             // the half is refilled by the async proxy next: order our reads first
@@ -625,6 +642,7 @@ __global__ void __launch_bounds__(PPR_NT) k_ppr_long(PprArgs A) {
     extern __shared__ float ppr_sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float* dz = warp_dz(ppr_sm, A.s_in, warp, lane);
+    const uint32_t amask = active_mask<C>(A, lane);
     const uint32_t gw = blockIdx.x * PPR_WARPS + warp, nw = gridDim.x * PPR_WARPS;
     for (uint32_t k = gw; k < A.n_long; k += nw) {
         const uint4 lr = A.longs[k];
@@ -642,7 +660,7 @@ __global__ void __launch_bounds__(PPR_NT) k_ppr_long(PprArgs A) {
         float sum[C];
 #pragma unroll
         for (int q = 0; q < C; ++q) sum[q] = t[q].value();
-        finish_row<C>(A, lr.x, r, sum, lane, dz);
+        finish_row<C>(A, lr.x, r, sum, lane, dz, amask);
     }
     // seed rows without in-edges: an empty sum
     for (uint32_t k = gw; k < A.n_eseeds; k += nw) {
@@ -652,7 +670,7 @@ __global__ void __launch_bounds__(PPR_NT) k_ppr_long(PprArgs A) {
         float sum[C];
 #pragma unroll
         for (int q = 0; q < C; ++q) sum[q] = 0.f;
-        finish_row<C>(A, v, r, sum, lane, dz);
+        finish_row<C>(A, v, r, sum, lane, dz, amask);
     }
     cta_fold<C>(A, ppr_sm, PPR_WARPS, A.s_in);
 }
