@@ -52,3 +52,33 @@ def test_one_rank_needs_no_process_group():
     import bench
     assert bench.max_over_ranks(12.5, 1) == 12.5
     assert bench.whole_job_gteps(1, 10, 3, 1000.0) == 10 * 3 / 1.0 / 1e9
+
+
+def test_clock_samples_outside_the_timed_region_are_dropped():
+    # bench.Clocks keeps only the nvidia-smi samples stamped inside the timed
+    # region, and reports a slowdown reason seen in any of them
+    import datetime
+    import sys
+    import time
+    sys.path.insert(0, ROOT)
+    import bench
+
+    def stamp(t):
+        return datetime.datetime.fromtimestamp(t).strftime("%Y/%m/%d %H:%M:%S.%f")[:-3]
+
+    now = time.time()
+    c = bench.Clocks(0)
+    c.lines = [
+        f"{stamp(now - 2)}, 1100, 2070, 300.0, Not Active, Not Active, Not Active, Not Active",
+        f"{stamp(now + 0.05)}, 2070, 2070, 900.0, Not Active, Not Active, Not Active, Active",
+        f"{stamp(now + 0.10)}, 2040, 2070, 950.0, Not Active, Not Active, Not Active, Not Active",
+        f"{stamp(now + 0.15)}, [N/A], 2070, 950.0, Not Active, Not Active, Not Active, Not Active",
+        f"{stamp(now + 9)}, 900, 2070, 200.0, Active, Not Active, Not Active, Not Active",
+    ]
+    c.t0, c.t1 = now, now + 1.0
+    s = c.summary()
+    assert s["samples"] == 2
+    assert s["sm_mhz"] == 2055.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    c.t0, c.t1 = now + 5, now + 6  # nothing inside: no summary
+    assert c.summary() is None
