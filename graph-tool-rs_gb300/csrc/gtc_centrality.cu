@@ -126,6 +126,21 @@ __global__ void k_seed(uint32_t n, const uint32_t* __restrict__ perm, uint64_t h
     x64[i] = v < had ? ld_any(x, xdt, v) : (pers ? ld_any(pers, pdt, v) : uniform);
 }
 
+// k_seed's pick for internal slot i (vertex o = perm[i]), rounded to FP32.
+__device__ __forceinline__ float seed_f32(uint32_t o, uint64_t had, const void* __restrict__ x,
+                                          int xdt, const void* __restrict__ pers, int pdt,
+                                          float uniform) {
+    return o < had ? ld_f32(x, xdt, o) : (pers ? ld_f32(pers, pdt, o) : uniform);
+}
+
+// The initial iterate straight into FP32, for a loop that keeps no FP64 copy.
+__global__ void k_seed_f32(uint32_t n, const uint32_t* __restrict__ perm, uint64_t had,
+                           const void* __restrict__ x, int xdt, const void* __restrict__ pers,
+                           int pdt, float uniform, float* __restrict__ y) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = seed_f32(perm[i], had, x, xdt, pers, pdt, uniform);
+}
+
 // FP32 copy; with `perm` the source is in original labels.
 __global__ void k_to_f32(uint32_t n, const void* __restrict__ x, int xdt,
                          const uint32_t* __restrict__ perm, float* __restrict__ y) {
@@ -161,6 +176,31 @@ __global__ void __launch_bounds__(PR_NT) k_pr_prime(uint32_t n, const float* __r
         float x = r[v];
         y[v] = __fmul_rn(x, invdeg[v]);
         if (sink[v]) sacc.add(x);
+    }
+    block_fold_exact<PR_NT>(none, sacc, f);
+}
+
+// The FP32 PageRank loop's first iterate in one pass: r = the initial iterate
+// rounded to FP32 (from x64 when given, else picked as k_seed picks it),
+// y = r * invdeg, yz = 0 on the dangling rows (a sweep stores no y there),
+// entry n of both gathered vectors 0 (the slices' padding gathers it), and
+// the dangling mass of r summed exactly.
+__global__ void __launch_bounds__(PR_NT) k_pr_seed(
+    uint32_t n, const double* __restrict__ x64, const uint32_t* __restrict__ perm, uint64_t had,
+    const void* __restrict__ x, int xdt, const void* __restrict__ pers, int pdt, float uniform,
+    const float* __restrict__ invdeg, const uint8_t* __restrict__ sink, float* __restrict__ r,
+    float* __restrict__ y, float* __restrict__ yz, ExactFold f) {
+    ExactPR none, sacc;
+    if (blockIdx.x == 0 && threadIdx.x == 0) y[n] = 0.f, yz[n] = 0.f;
+    for (size_t v = (size_t)blockIdx.x * PR_NT + threadIdx.x; v < n;
+         v += (size_t)gridDim.x * PR_NT) {
+        const float xv = x64 ? (float)x64[v] : seed_f32(perm[v], had, x, xdt, pers, pdt, uniform);
+        r[v] = xv;
+        y[v] = __fmul_rn(xv, invdeg[v]);
+        if (sink[v]) {
+            yz[v] = 0.f;
+            sacc.add(xv);
+        }
     }
     block_fold_exact<PR_NT>(none, sacc, f);
 }
@@ -818,20 +858,68 @@ const float* cached_sliced_weights(gtc_graph* g, WeightCache& c, int k, const Un
     return c.sliced[k].get();
 }
 
+// Out-degrees of the unweighted, unfiltered view over the in-halves (h = 0,
+// the reversed view) or the out-halves (h = 1, the plain view), kept on the
+// handle.
+void cached_plain_degrees(gtc_graph* g, int h, uint64_t* L, const double** deg,
+                          const uint8_t** sink) {
+    const uint32_t n = g->n;
+    DegCache& c = g->dcache;
+    if (!c.deg[h].get()) {
+        c.deg[h].alloc(n, g->home);
+        c.sink[h].alloc(n, g->home);
+        const Halves& hv = h ? g->out : g->in;
+        if (n) {
+            k_degree<<<grid_for(n, 256, 1u << 30), 256, 0, g->home>>>(
+                n, hv.off.get(), hv.eid.get(), nullptr, GTC_F64, nullptr, c.deg[h].get(),
+                c.sink[h].get());
+            GTC_LAUNCHED();
+            (*L)++;
+        }
+        GTC_CUDA(cudaStreamSynchronize(g->home));
+    }
+    *deg = c.deg[h].get();
+    *sink = c.sink[h].get();
+}
+
 // Everything a sweep loop needs that does not change between sweeps.
 struct Prep {
     View view;
     double uniform = 0.0;
     DevBuf<double> deg;
     DevBuf<uint8_t> sink;
-    const double* degp = nullptr;   // deg, or the handle's cached weighted degrees
+    DevBuf<float> invdeg;
+    const double* degp = nullptr;   // deg, or the handle's cached degrees
     const uint8_t* sinkp = nullptr;
+    DevBuf<float>* inv_cache = nullptr;  // the handle's FP32 inverse of cached degrees
     WeightCache* wc = nullptr;      // the handle's weight layouts (FP32, unfiltered, weighted)
-    DevBuf<double> x64;  // initial iterate, FP64
+    DevBuf<double> x64;  // initial iterate, FP64 (left empty when the caller seeds FP32)
 };
 
+// The FP32 inverse degrees of the view: kept on the handle beside cached
+// degrees, else computed for this call.
+const float* invdeg_f32(gtc_graph* g, Prep& P, cudaStream_t s, uint64_t* L) {
+    const uint32_t n = P.view.n;
+    DevBuf<float>& b = P.inv_cache ? *P.inv_cache : P.invdeg;
+    if (!b.get()) {
+        // cached degrees were written on the home stream, which is idle
+        cudaStream_t st = P.inv_cache ? g->home : s;
+        b.alloc(n, st);
+        if (n) {
+            k_invdeg_f32<<<grid_for(n, 256, 1u << 30), 256, 0, st>>>(n, P.degp, b.get());
+            GTC_LAUNCHED();
+            (*L)++;
+        }
+        if (P.inv_cache) GTC_CUDA(cudaStreamSynchronize(g->home));
+    }
+    return b.get();
+}
+
+// seed_x64 false: the caller seeds its FP32 iterate itself (k_pr_seed or
+// k_seed_f32) and P.x64 stays empty; only an unfiltered view may skip it,
+// since k_store reads x64 for the vertices a filter leaves out.
 void prepare(gtc_graph* g, const gtc_view* vw, const SolveIn& in, bool need_deg, Prep& P,
-             cudaStream_t s, uint64_t* L) {
+             cudaStream_t s, uint64_t* L, bool seed_x64 = true) {
     const unsigned TB = 256;
     P.view.prepare(g, vw, s, L);
     const uint32_t n = P.view.n;
@@ -840,8 +928,13 @@ void prepare(gtc_graph* g, const gtc_view* vw, const SolveIn& in, bool need_deg,
         const unsigned long long h = scan_weights(in.weight, g->m, s, L);
         if (in.precision == GTC_PREC_F32 && !P.view.filtered) P.wc = &weight_cache(g, in.weight, h);
     }
+    const int hd = P.view.reversed ? 0 : 1;  // the halves the view pushes over
     if (need_deg && P.wc) {
-        cached_degrees(g, *P.wc, P.view.reversed ? 0 : 1, s, L, &P.degp, &P.sinkp);
+        cached_degrees(g, *P.wc, hd, s, L, &P.degp, &P.sinkp);
+        P.inv_cache = &P.wc->invdeg[hd];
+    } else if (need_deg && !in.weight.present() && !P.view.filtered) {
+        cached_plain_degrees(g, hd, L, &P.degp, &P.sinkp);
+        P.inv_cache = &g->dcache.invdeg[hd];
     } else if (need_deg) {
         P.deg.alloc(n, s);
         P.sink.alloc(n, s);
@@ -866,6 +959,7 @@ void prepare(gtc_graph* g, const gtc_view* vw, const SolveIn& in, bool need_deg,
             (*L)++;
         }
     }
+    if (!seed_x64 && !P.view.filtered) return;
     P.x64.alloc(n, s);
     if (n) {
         k_seed<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, g->perm.get(), in.had, in.x, in.x_dtype,
@@ -929,7 +1023,7 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
     uint64_t L = 0, SL = 0;
     const unsigned TB = 256;
     Prep P;
-    prepare(g, vw, in, true, P, s, &L);
+    prepare(g, vw, in, true, P, s, &L, in.precision == GTC_PREC_F64_EXACT);
     const View& view = P.view;
     const uint32_t n = view.n;
     const double d = in.damping;
@@ -1014,12 +1108,7 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         res->device_ms = total.ms();
         store_result<double>(g, n, cur, P, in, s, &L);
     } else {
-        DevBuf<float> invdeg(n, s);
-        if (n) {
-            k_invdeg_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.degp, invdeg.get());
-            GTC_LAUNCHED();
-            L++;
-        }
+        const float* invdeg = invdeg_f32(g, P, s, &L);
         DevBuf<float> pers32;
         if (in.pers.present() && n) {
             pers32.alloc(n, s);
@@ -1029,23 +1118,16 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
             L++;
         }
         // the gathered vectors carry one more entry, kept 0: the slices'
-        // padding gathers it
-        // (a sweep does not store y of a dangling row: it stays 0, from the
-        // prime in y0 and from this clear in y1)
+        // padding gathers it (a sweep does not store y of a dangling row
+        // either: k_pr_seed zeroes those in y1)
         DevBuf<float> r0(n, s), r1(n, s), y0((size_t)n + 1, s), y1((size_t)n + 1, s);
-        GTC_CUDA(cudaMemsetAsync(y0.get() + n, 0, sizeof(float), s));
-        GTC_CUDA(cudaMemsetAsync(y1.get(), 0, ((size_t)n + 1) * sizeof(float), s));
-        if (n) {
-            k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.x64.get(), GTC_F64, nullptr,
-                                                              r0.get());
-            GTC_LAUNCHED();
-            L++;
-        }
         const unsigned nb = persistent_blocks(n);
         FoldBufs fb(nb, s);
         double* dp = fb.out.get();  // [0] delta, [1] dangling mass of the current iterate
-        k_pr_prime<<<nb, PR_NT, 0, s>>>(n, r0.get(), invdeg.get(), P.sinkp, y0.get(),
-                                       fb.fold(dp + 2, dp + 1));
+        k_pr_seed<<<nb, PR_NT, 0, s>>>(n, P.x64.get(), g->perm.get(), in.had, in.x, in.x_dtype,
+                                      in.pers.p, in.pers.dtype, (float)P.uniform, invdeg,
+                                      P.sinkp, r0.get(), y0.get(), y1.get(),
+                                      fb.fold(dp + 2, dp + 1));
         GTC_LAUNCHED();
         L++;
         float *rc = r0.get(), *rn = r1.get(), *yc = y0.get(), *yn = y1.get();
@@ -1063,7 +1145,7 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         A.sw = sw8.sliced;
         A.w = sw8.pull;
         A.active = act;
-        A.invdeg = invdeg.get();
+        A.invdeg = invdeg;
         A.sink = P.sinkp;
         A.pers = pers32.get();
         A.uniform = (float)P.uniform;
@@ -1122,7 +1204,7 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
                  cudaStream_t s) {
     uint64_t L = 0, SL = 0;
     Prep P;
-    prepare(g, vw, in, false, P, s, &L);
+    prepare(g, vw, in, false, P, s, &L, in.precision == GTC_PREC_F64_EXACT);
     const View& view = P.view;
     const uint32_t n = view.n;
     const uint8_t* act = view.active_or_null();
@@ -1177,9 +1259,15 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         DevBuf<float> x0((size_t)n + 1, s), x1((size_t)n + 1, s);  // x[n] == 0: slice padding
         GTC_CUDA(cudaMemsetAsync(x0.get() + n, 0, sizeof(float), s));
         GTC_CUDA(cudaMemsetAsync(x1.get() + n, 0, sizeof(float), s));
-        if (n) {
+        if (n && P.x64.get()) {
             k_to_f32<<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, P.x64.get(), GTC_F64, nullptr,
                                                                 x0.get());
+            GTC_LAUNCHED();
+            L++;
+        } else if (n) {
+            k_seed_f32<<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(
+                n, g->perm.get(), in.had, in.x, in.x_dtype, in.pers.p, in.pers.dtype,
+                (float)P.uniform, x0.get());
             GTC_LAUNCHED();
             L++;
         }
@@ -1370,6 +1458,7 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     if (W && P.wc) {
         wpull = cached_half_weights(g, *P.wc, hav, s, &L);
         cached_degrees(g, *P.wc, hav, s, &L, &P.degp, &P.sinkp);
+        P.inv_cache = &P.wc->invdeg[hav];
     } else if (W) {
         if (av.m_pull) {
             wpull_own.alloc(av.m_pull, s);
@@ -1390,14 +1479,14 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
             L++;
         }
     }
-    DevBuf<float> invdeg(n, s), pers32, g32(n, s), pi32(n, s), ypi((size_t)n + 1, s);
+    const float* invdeg = invdeg_f32(g, P, s, &L);
+    DevBuf<float> pers32, g32(n, s), pi32(n, s), ypi((size_t)n + 1, s);
     if (n) {
-        k_invdeg_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.degp, invdeg.get());
         k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, P.x64.get(), GTC_F64, nullptr, pi32.get());
         k_to_f32<<<grid_for(n, TB, 1u << 30), TB, 0, s>>>(n, in.gpi.p, in.gpi.dtype, g->perm.get(),
                                                           g32.get());
         GTC_LAUNCHED();
-        L += 3;
+        L += 2;
     }
     if (in.pers.present() && n) {
         pers32.alloc(n, s);
@@ -1410,7 +1499,7 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     FoldBufs fb(nb, s);
     double* dp = fb.out.get();  // [1] dangling mass of pi
     // y = pi / deg and the dangling mass of pi
-    k_pr_prime<<<nb, PR_NT, 0, s>>>(n, pi32.get(), invdeg.get(), P.sinkp, ypi.get(),
+    k_pr_prime<<<nb, PR_NT, 0, s>>>(n, pi32.get(), invdeg, P.sinkp, ypi.get(),
                                    fb.fold(dp + 2, dp + 1));
     GTC_LAUNCHED();
     L++;
@@ -1452,7 +1541,7 @@ void pagerank_adjoint(gtc_graph* g, const gtc_view* vw, const AdjointIn& in, gtc
     }
     A.sw = swt;
     A.w = wpull;
-    A.invdeg = invdeg.get();
+    A.invdeg = invdeg;
     A.sink = P.sinkp;
     A.pers = pers32.get();
     A.gvec = g32.get();

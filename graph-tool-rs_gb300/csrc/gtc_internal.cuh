@@ -140,11 +140,21 @@ struct WeightCache {
     DevBuf<float> sliced[2];    // sliced entries of units_in [0] / units_out [1]
     DevBuf<double> deg[2];      // weighted degree over the in-halves [0] / out-halves [1]
     DevBuf<uint8_t> sink[2];    // zero weighted degree
+    DevBuf<float> invdeg[2];    // FP32 inverse of deg (0 on the sinks)
     void reset() {
         for (int h = 0; h < 2; ++h) half[h].release(), sliced[h].release(), deg[h].release(),
-                                    sink[h].release();
+                                    sink[h].release(), invdeg[h].release();
         valid = false;
     }
+};
+
+// Degrees of the unweighted, unfiltered views over the in-halves [0] (the
+// reversed view's out-degree) and the out-halves [1] (the plain view's):
+// they depend on the graph alone, so the handle keeps them.
+struct DegCache {
+    DevBuf<double> deg[2];      // out-degree of the view, FP64
+    DevBuf<uint8_t> sink[2];    // out-degree 0
+    DevBuf<float> invdeg[2];    // FP32 inverse of deg (0 on the sinks)
 };
 
 // Pull schedule of the batched personalised PageRank (gtc_ppr.cu): rows with
@@ -247,6 +257,7 @@ struct gtc_graph {
     gtc::Halves in;   // CSC: in-halves (in_edges order, the pull order)
     gtc::Units units_in, units_out;  // pull schedules of the plain and reversed views
     gtc::WeightCache wcache;         // FP32 weight layouts of the last weight map used
+    gtc::DegCache dcache;            // unweighted degrees of the plain and reversed views
     gtc::PprSched ppr_sched[2];      // batched schedules of the plain and reversed views
     gtc::DevBuf<float> ppr_z[2];     // batched iterates, kept between calls (grown on demand)
     uint64_t launches = 0;  // kernels this handle has launched (diagnostics)
