@@ -133,12 +133,19 @@ __device__ __forceinline__ float seed_f32(uint32_t o, uint64_t had, const void* 
     return o < had ? ld_f32(x, xdt, o) : (pers ? ld_f32(pers, pdt, o) : uniform);
 }
 
-// The initial iterate straight into FP32, for a loop that keeps no FP64 copy.
+// The initial iterate straight into FP32, for a loop that keeps no FP64 copy
+// (perm null: no map is read, every slot is seeded uniform).
 __global__ void k_seed_f32(uint32_t n, const uint32_t* __restrict__ perm, uint64_t had,
                            const void* __restrict__ x, int xdt, const void* __restrict__ pers,
                            int pdt, float uniform, float* __restrict__ y) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = seed_f32(perm[i], had, x, xdt, pers, pdt, uniform);
+    if (i < n) y[i] = perm ? seed_f32(perm[i], had, x, xdt, pers, pdt, uniform) : uniform;
+}
+
+// The label map k_seed_f32 and k_pr_seed read the caller's maps through: none
+// when no map is read.
+inline const uint32_t* seed_perm(const gtc_graph* g, const SolveIn& in) {
+    return (in.had > 0 || in.pers.present()) ? g->perm.get() : nullptr;
 }
 
 // FP32 copy; with `perm` the source is in original labels.
@@ -184,7 +191,8 @@ __global__ void __launch_bounds__(PR_NT) k_pr_prime(uint32_t n, const float* __r
 // rounded to FP32 (from x64 when given, else picked as k_seed picks it),
 // y = r * invdeg, yz = 0 on the dangling rows (a sweep stores no y there),
 // entry n of both gathered vectors 0 (the slices' padding gathers it), and
-// the dangling mass of r summed exactly.
+// the dangling mass of r summed exactly.  perm null: no map is read, every
+// slot is seeded uniform.
 __global__ void __launch_bounds__(PR_NT) k_pr_seed(
     uint32_t n, const double* __restrict__ x64, const uint32_t* __restrict__ perm, uint64_t had,
     const void* __restrict__ x, int xdt, const void* __restrict__ pers, int pdt, float uniform,
@@ -194,7 +202,9 @@ __global__ void __launch_bounds__(PR_NT) k_pr_seed(
     if (blockIdx.x == 0 && threadIdx.x == 0) y[n] = 0.f, yz[n] = 0.f;
     for (size_t v = (size_t)blockIdx.x * PR_NT + threadIdx.x; v < n;
          v += (size_t)gridDim.x * PR_NT) {
-        const float xv = x64 ? (float)x64[v] : seed_f32(perm[v], had, x, xdt, pers, pdt, uniform);
+        const float xv = x64    ? (float)x64[v]
+                         : perm ? seed_f32(perm[v], had, x, xdt, pers, pdt, uniform)
+                                : uniform;
         r[v] = xv;
         y[v] = __fmul_rn(xv, invdeg[v]);
         if (sink[v]) {
@@ -1124,9 +1134,9 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         const unsigned nb = persistent_blocks(n);
         FoldBufs fb(nb, s);
         double* dp = fb.out.get();  // [0] delta, [1] dangling mass of the current iterate
-        k_pr_seed<<<nb, PR_NT, 0, s>>>(n, P.x64.get(), g->perm.get(), in.had, in.x, in.x_dtype,
-                                      in.pers.p, in.pers.dtype, (float)P.uniform, invdeg,
-                                      P.sinkp, r0.get(), y0.get(), y1.get(),
+        k_pr_seed<<<nb, PR_NT, 0, s>>>(n, P.x64.get(), seed_perm(g, in), in.had, in.x,
+                                      in.x_dtype, in.pers.p, in.pers.dtype, (float)P.uniform,
+                                      invdeg, P.sinkp, r0.get(), y0.get(), y1.get(),
                                       fb.fold(dp + 2, dp + 1));
         GTC_LAUNCHED();
         L++;
@@ -1266,7 +1276,7 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
             L++;
         } else if (n) {
             k_seed_f32<<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(
-                n, g->perm.get(), in.had, in.x, in.x_dtype, in.pers.p, in.pers.dtype,
+                n, seed_perm(g, in), in.had, in.x, in.x_dtype, in.pers.p, in.pers.dtype,
                 (float)P.uniform, x0.get());
             GTC_LAUNCHED();
             L++;

@@ -191,3 +191,39 @@ def test_f32_eigenvector_rel_l1(oracle, gtc, er10k):
     print(f"eigen f32: rel L1 {err:.3e}, eig {eg} vs {ew}, sweeps {ig} vs {iw}")
     assert err < 1e-6
     assert abs(eg - ew) / ew < 1e-6
+
+
+def test_handle_caches_keep_results_bitwise(gtc, er10k):
+    """The graph handle keeps the unweighted degrees, the FP32 inverse degrees
+    and the weight layouts of its plain and reversed views between calls: a
+    sequence of solves on one graph gives, call by call, bitwise what a
+    fresh graph gives."""
+    n, src, tgt = er10k
+    w = np.random.default_rng(21).uniform(0.1, 1.0, src.size)
+    start = np.random.default_rng(22).uniform(0, 2.0 / n, n)
+    G = K.GpuSolver(gtc, "f32")
+    shared = G.graph(n, src, tgt)
+    seq = [("pr", dict()), ("pr", dict(reversed=True)), ("pr", dict(weight=w)), ("ev", dict()),
+           ("pr", dict()), ("pr", dict(weight=w, reversed=True)), ("pr", dict(reversed=True)),
+           ("pr", dict(precision="f64_exact")), ("pr", dict(rank=start)), ("ev", dict(weight=w)),
+           ("pr", dict(weight=w))]
+
+    def run(g, what, kw):
+        kw = dict(kw)
+        prec = kw.pop("precision", "f32")
+        r = g.new_vertex_property("double")
+        if "rank" in kw:
+            r._a = kw.pop("rank").copy()
+        if what == "pr":
+            res = g.pagerank(r, epsilon=1e-7, max_iter=500, grain=4096, precision=prec,
+                             result=True, **kw)
+        else:
+            res = g.eigenvector(r, epsilon=1e-7, max_iter=500, grain=4096, precision=prec,
+                                result=True, **kw)
+        return r.a.copy(), int(res.iterations)
+
+    for what, kw in seq:
+        a, ia = run(shared, what, kw)
+        b, ib = run(G.graph(n, src, tgt), what, kw)
+        assert ia == ib, (what, sorted(kw), ia, ib)
+        assert a.tobytes() == b.tobytes(), (what, sorted(kw), np.max(np.abs(a - b)))
