@@ -232,6 +232,90 @@ __device__ __forceinline__ void plan_range(uint64_t n, uint64_t chunks, uint64_t
 // k_ev_f64_long); shorter rows by a thread each.
 constexpr uint32_t F64_SHORT = 32;
 
+// FP64 on this GPU: an add has a latency of about 64 cycles, and a warp
+// instruction costs the FP64 pipe the same whether one lane or 32 are active
+// (about 80 cycles of a sub-partition's pipe).  So a sequential fold (the
+// reference's left fold, which fixes the bits) is cheapest with one chain
+// per lane -- a thread per row or per chunk -- and its latency is hidden by
+// keeping the next terms' loads in flight while a block of terms is added.
+
+// acc + term(b) + term(b + 1) + ... + term(e - 1), added left to right.
+// idx(p) loads the index of entry p, val(j) the term of index j.  While a
+// block of FU terms is added, the terms of the next FD blocks and the
+// indices of the one after those are loading, so a long chain of adds waits
+// on no load (FD blocks of adds take longer than a gather from DRAM).
+constexpr int FU = 8;
+template <int FD, class Idx, class Val>
+__device__ __forceinline__ double fold_seq(double acc, uint64_t b, uint64_t e, Idx&& idx,
+                                           Val&& val) {
+    double t[FD + 1][FU];
+    uint32_t sn[FU];
+#pragma unroll
+    for (int k = 0; k < FD; ++k)
+#pragma unroll
+        for (int j = 0; j < FU; ++j) {
+            const uint64_t p = b + (uint64_t)k * FU + j;
+            const uint32_t si = p < e ? idx(p) : 0u;
+            t[k][j] = p < e ? val(si) : 0.0;
+        }
+#pragma unroll
+    for (int j = 0; j < FU; ++j) {
+        const uint64_t p = b + (uint64_t)FD * FU + j;
+        sn[j] = p < e ? idx(p) : 0u;
+    }
+    for (uint64_t p = b; p < e; p += FU) {
+#pragma unroll
+        for (int j = 0; j < FU; ++j) t[FD][j] = p + FD * FU + j < e ? val(sn[j]) : 0.0;
+#pragma unroll
+        for (int j = 0; j < FU; ++j) sn[j] = p + (FD + 1) * FU + j < e ? idx(p + (FD + 1) * FU + j) : 0u;
+#pragma unroll
+        for (int j = 0; j < FU; ++j)
+            if (p + j < e) acc = __dadd_rn(acc, t[0][j]);
+#pragma unroll
+        for (int k = 0; k < FD; ++k)
+#pragma unroll
+            for (int j = 0; j < FU; ++j) t[k][j] = t[k + 1][j];
+    }
+    return acc;
+}
+
+// Unweighted views: the reference's term (prev[s] * 1.0) / ds is prev[s] / ds,
+// one value per source, so it is formed once per sweep here instead of once
+// per edge.  Every source an active row gathers has ds >= 1 (in the view it
+// keeps at least its edge into that row), so the reference's ds != 0 test
+// never skips a term of these rows.
+__global__ void k_pr_f64_q(uint32_t n, const double* __restrict__ prev,
+                           const double* __restrict__ deg, double* __restrict__ q) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) q[i] = deg[i] != 0.0 ? __ddiv_rn(prev[i], deg[i]) : 0.0;
+}
+
+// Unweighted rows, every length: a thread per row folds q over its in-edges
+// in storage order (centrality.rs:355-365).
+__global__ void __launch_bounds__(128) k_pr_f64_rows_q(
+    uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ other,
+    const double* __restrict__ q, const uint8_t* __restrict__ active,
+    const double* __restrict__ pers, double uniform, double one_minus_d, double d,
+    const double* __restrict__ psink_p, const double* __restrict__ prev,
+    double* __restrict__ next, double* __restrict__ diff) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (active && !active[i]) {
+        next[i] = prev[i];
+        diff[i] = 0.0;
+        return;
+    }
+    const double pv = pers ? pers[i] : uniform;
+    double r = __dmul_rn(*psink_p, pv);
+    // one block of lookahead: deeper ones cost the short rows occupancy (a
+    // long row's chain is bound by the FP64 pipe, not by its loads)
+    r = fold_seq<1>(r, off[i], off[i + 1], [&](uint64_t p) { return other[p]; },
+                 [&](uint32_t src) { return q[src]; });
+    const double nv = __dadd_rn(__dmul_rn(one_minus_d, pv), __dmul_rn(d, r));
+    diff[i] = fabs(__dsub_rn(nv, prev[i]));
+    next[i] = nv;
+}
+
 // acc + t(lane 0) + t(lane 1) + ... + t(lane 31), left to right, skipping the
 // lanes whose bit of `valid` is clear: the sequential fold of 32 terms the
 // lanes computed in parallel.  Every lane ends with the same acc.
@@ -319,23 +403,20 @@ __global__ void k_pr_f64_long(uint32_t n, const uint32_t* __restrict__ off,
     }
 }
 
-// Plan-chunk partials: a warp per chunk folds it sequentially from 0.0
-// (lanes load 32 values at a time; the adds run in index order).
-__global__ void k_chunk_sums(uint64_t n, uint64_t chunks, const double* __restrict__ v,
-                             const uint32_t* __restrict__ gather, double* __restrict__ part) {
-    const unsigned lane = threadIdx.x & 31;
-    const uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (k >= chunks) return;  // whole warps leave together
+// Plan-chunk partials: a thread per chunk folds it sequentially from 0.0, in
+// index order (values through `gather` when given).
+__global__ void __launch_bounds__(32) k_chunk_sums(uint64_t n, uint64_t chunks,
+                                                   const double* __restrict__ v,
+                                                   const uint32_t* __restrict__ gather,
+                                                   double* __restrict__ part) {
+    const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= chunks) return;
     uint64_t s, e;
     plan_range(n, chunks, k, s, e);
-    double acc = 0.0;
-    for (uint64_t base = s; base < e; base += 32) {
-        const uint64_t i = base + lane;
-        const bool ok = i < e;
-        const double t = ok ? (gather ? v[gather[i]] : v[i]) : 0.0;
-        acc = fold_lanes_in_order(acc, t, __ballot_sync(0xffffffffu, ok));
-    }
-    if (lane == 0) part[k] = acc;
+    part[k] = gather ? fold_seq<4>(0.0, s, e, [&](uint64_t i) { return gather[i]; },
+                                   [&](uint32_t j) { return v[j]; })
+                     : fold_seq<4>(0.0, s, e, [&](uint64_t i) { return (uint32_t)i; },
+                                   [&](uint32_t j) { return v[j]; });
 }
 
 // Left fold of the chunk partials from 0.0 (one warp, adds in order).  mode 0: out = sum;
@@ -393,6 +474,28 @@ __global__ void k_ev_f64_rows(uint32_t n, const uint32_t* __restrict__ off,
         const double we = w ? w[p] : 1.0;
         s = __dadd_rn(s, __dmul_rn(we, prev[other[p]]));
     }
+    next[i] = s;
+    sq[i] = __dmul_rn(s, s);
+}
+
+// Unweighted rows, every length: a thread per row folds prev over its
+// in-edges in storage order from 0.0 (the reference's 1.0 * prev[s] is
+// prev[s]).
+__global__ void __launch_bounds__(128) k_ev_f64_rows_u(uint32_t n, const uint32_t* __restrict__ off,
+                                                       const uint32_t* __restrict__ other,
+                                                       const uint8_t* __restrict__ active,
+                                                       const double* __restrict__ prev,
+                                                       double* __restrict__ next,
+                                                       double* __restrict__ sq) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (active && !active[i]) {
+        next[i] = prev[i];
+        sq[i] = 0.0;
+        return;
+    }
+    const double s = fold_seq<1>(0.0, off[i], off[i + 1], [&](uint64_t p) { return other[p]; },
+                                 [&](uint32_t src) { return prev[src]; });
     next[i] = s;
     sq[i] = __dmul_rn(s, s);
 }
@@ -1069,6 +1172,8 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         const uint64_t sink_chunks = std::max<uint64_t>((n_sinks + grain - 1) / grain, 1);
         DevBuf<double> wpull = pull_weights<double>(P, in, s, &L);
         DevBuf<double> scratch(n, s), diff(n, s), part(std::max(chunks, sink_chunks), s);
+        DevBuf<double> q;  // unweighted: the per-source terms of a sweep
+        if (!wpull.get()) q.alloc(n, s);
         DevBuf<double> scal(4, s);  // [p_sink, delta]
         const double* pers64 = nullptr;
         DevBuf<double> pbuf;
@@ -1088,10 +1193,15 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
         total.start();
         while (delta >= eps) {
             if (in.timing) sw.start();
-            k_chunk_sums<<<grid_for(sink_chunks * 32, 128, 1u << 30), 128, 0, s>>>(
+            k_chunk_sums<<<grid_for(sink_chunks, 32, 1u << 30), 32, 0, s>>>(
                 n_sinks, sink_chunks, cur, sinks.get(), part.get());
             k_fold<<<1, 32, 0, s>>>(sink_chunks, part.get(), scal.get(), nullptr, 0);
-            if (n) {
+            if (n && !wpull.get()) {
+                k_pr_f64_q<<<grid_for(n, 256, 1u << 30), 256, 0, s>>>(n, cur, P.degp, q.get());
+                k_pr_f64_rows_q<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(
+                    n, view.pull_off, view.pull_other, q.get(), act, pers64, P.uniform, 1.0 - d,
+                    d, scal.get(), cur, nxt, diff.get());
+            } else if (n) {
                 k_pr_f64_rows<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(
                     n, view.pull_off, view.pull_other, wpull.get(), P.degp, act, pers64,
                     P.uniform, 1.0 - d, d, scal.get(), cur, nxt, diff.get());
@@ -1100,7 +1210,7 @@ void pagerank(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result* r
                     P.uniform, 1.0 - d, d, scal.get(), cur, nxt, diff.get());
             }
             // the delta is folded over the Plan in original vertex order
-            k_chunk_sums<<<grid_for(chunks * 32, 128, 1u << 30), 128, 0, s>>>(n, chunks, diff.get(),
+            k_chunk_sums<<<grid_for(chunks, 32, 1u << 30), 32, 0, s>>>(n, chunks, diff.get(),
                                                                          g->iperm.get(), part.get());
             k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get() + 1, nullptr, 0);
             GTC_LAUNCHED();
@@ -1232,26 +1342,30 @@ void eigenvector(gtc_graph* g, const gtc_view* vw, const SolveIn& in, gtc_result
         total.start();
         while (delta >= eps) {
             if (in.timing) sw.start();
-            if (n) {
+            if (n && !wpull.get()) {
+                k_ev_f64_rows_u<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(
+                    n, view.pull_off, view.pull_other, act, cur, nxt, tmp.get());
+            } else if (n) {
                 k_ev_f64_rows<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(
                     n, view.pull_off, view.pull_other, wpull.get(), act, cur, nxt, tmp.get());
                 k_ev_f64_long<<<(unsigned)sm_count() * 8, 256, 0, s>>>(
                     n, view.pull_off, view.pull_other, wpull.get(), act, cur, nxt, tmp.get());
             }
-            k_chunk_sums<<<grid_for(chunks * 32, 128, 1u << 30), 128, 0, s>>>(n, chunks, tmp.get(),
+            k_chunk_sums<<<grid_for(chunks, 32, 1u << 30), 32, 0, s>>>(n, chunks, tmp.get(),
                                                                          g->iperm.get(), part.get());
             // scal[0] = squared norm, scal[1] = norm, scal[2] = scale
             k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get(), scal.get() + 2, 1);
             if (n)
                 k_ev_f64_norm<<<grid_for(n, 128, 1u << 30), 128, 0, s>>>(n, act, scal.get() + 2,
                                                                          cur, nxt, tmp.get());
-            k_chunk_sums<<<grid_for(chunks * 32, 128, 1u << 30), 128, 0, s>>>(n, chunks, tmp.get(),
+            k_chunk_sums<<<grid_for(chunks, 32, 1u << 30), 32, 0, s>>>(n, chunks, tmp.get(),
                                                                          g->iperm.get(), part.get());
             k_fold<<<1, 32, 0, s>>>(chunks, part.get(), scal.get() + 3, nullptr, 0);
             GTC_LAUNCHED();
             if (in.timing) sw.stop();
-            L += n ? 7 : 4;
-            SL += n ? 7 : 4;
+            const uint64_t per_sweep = n ? (wpull.get() ? 7 : 6) : 4;
+            L += per_sweep;
+            SL += per_sweep;
             double hs[4];
             GTC_CUDA(cudaMemcpyAsync(hs, scal.get(), 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
             GTC_CUDA(cudaStreamSynchronize(s));
