@@ -227,3 +227,25 @@ def test_handle_caches_keep_results_bitwise(gtc, er10k):
         b, ib = run(G.graph(n, src, tgt), what, kw)
         assert ia == ib, (what, sorted(kw), ia, ib)
         assert a.tobytes() == b.tobytes(), (what, sorted(kw), np.max(np.abs(a - b)))
+
+
+def test_exact_bit_identical_with_long_rows(oracle, gtc):
+    """Rows of hundreds to thousands of in-edges (an R-MAT hub), unweighted
+    and weighted, plain and reversed: the exact path's per-row folds and Plan
+    partials keep the reference's bits."""
+    from graph_tool import synth
+    n, src, tgt = synth.rmat_cpu(12, edge_factor=16, seed=3)
+    assert np.bincount(tgt, minlength=n).max() > 500
+    w = np.random.default_rng(4).uniform(0.1, 1.0, src.size)
+    O = K.OracleSolver(oracle)
+    G = K.GpuSolver(gtc, "f64_exact")
+    for kw in (dict(), dict(weight=w), dict(reversed=True), dict(weight=w, reversed=True)):
+        for grain in (64, 1000):
+            a, ia = O.pagerank(n, src, tgt, grain=grain, epsilon=1e-12, max_iter=60, **kw)
+            b, ib = G.pagerank(n, src, tgt, grain=grain, epsilon=1e-12, max_iter=60, **kw)
+            assert ia == ib, (sorted(kw), grain, ia, ib)
+            assert a.tobytes() == b.tobytes(), (sorted(kw), grain, np.max(np.abs(a - b)))
+        a, ea, ia = O.eigenvector(n, src, tgt, grain=64, epsilon=1e-10, max_iter=60, **kw)
+        b, eb, ib = G.eigenvector(n, src, tgt, grain=64, epsilon=1e-10, max_iter=60, **kw)
+        assert ia == ib and ea == eb, (sorted(kw), ia, ib, ea, eb)
+        assert a.tobytes() == b.tobytes(), sorted(kw)
