@@ -16,7 +16,9 @@ edges x sweeps / seconds / 1e9.
             events around K steps on the library's stream.
   e2e       the reference-facing C ABI call gtc_pagerank with host FP64
             buffers: the warm-start map (8n bytes) goes in and the result
-            (8n bytes) comes back every step, from pinned memory.
+            (8n bytes) comes back every step, from pinned memory; the calls
+            (synchronous) are timed one by one by wall clock, and the caller
+            refills its map with 1/n between them.
   roofline  the sweep kernel: algorithmic bytes per sweep (below) over its
             CUDA-event duration (gtc_options.timing), against the measured
             HBM copy bandwidth.
