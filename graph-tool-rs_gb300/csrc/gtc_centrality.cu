@@ -381,19 +381,28 @@ __global__ void k_pr_f64_long(uint32_t n, const uint32_t* __restrict__ off,
         }
         const double pv = pers ? pers[i] : uniform;
         double r = __dmul_rn(*psink_p, pv);
+        // Lane l's entry of chunk k is b + 32k + l.  While chunk k is folded,
+        // chunk k + 1's gathers and chunk k + 2's sources are loading; chunk
+        // k + 1's terms are formed after the fold, once those have arrived.
+        auto src_at = [&](uint32_t p) { return p < e ? other[p] : 0u; };
+        auto term = [&](uint32_t p, double pr, double ds, bool& ok) {
+            ok = p < e && ds != 0.0;
+            return ok ? __ddiv_rn(__dmul_rn(pr, w ? w[p] : 1.0), ds) : 0.0;
+        };
+        bool ok;
+        double t;
+        {
+            const uint32_t p = b + lane, s0 = src_at(p);
+            t = term(p, p < e ? prev[s0] : 0.0, p < e ? deg[s0] : 0.0, ok);
+        }
+        uint32_t s1 = src_at(b + 32 + lane);
         for (uint32_t base = b; base < e; base += 32) {
-            const uint32_t p = base + lane;
-            double t = 0.0;
-            bool ok = false;
-            if (p < e) {
-                const uint32_t src = other[p];
-                const double ds = deg[src];
-                if (ds != 0.0) {
-                    t = __ddiv_rn(__dmul_rn(prev[src], w ? w[p] : 1.0), ds);
-                    ok = true;
-                }
-            }
+            const uint32_t p1 = base + 32 + lane;
+            const double pr1 = p1 < e ? prev[s1] : 0.0, ds1 = p1 < e ? deg[s1] : 0.0;
+            const uint32_t s2 = src_at(base + 64 + lane);
             r = fold_lanes_in_order(r, t, __ballot_sync(0xffffffffu, ok));
+            t = term(p1, pr1, ds1, ok);
+            s1 = s2;
         }
         if (lane == 0) {
             const double nv = __dadd_rn(__dmul_rn(one_minus_d, pv), __dmul_rn(d, r));
@@ -515,12 +524,26 @@ __global__ void k_ev_f64_long(uint32_t n, const uint32_t* __restrict__ off,
             if (lane == 0) next[i] = prev[i], sq[i] = 0.0;
             continue;
         }
+        // chunk k + 1's gathers and chunk k + 2's sources load while chunk k
+        // is folded (as in k_pr_f64_long)
+        auto src_at = [&](uint32_t p) { return p < e ? other[p] : 0u; };
+        auto term = [&](uint32_t p, double pr) {
+            return p < e ? __dmul_rn(w ? w[p] : 1.0, pr) : 0.0;
+        };
         double s = 0.0;
+        double t;
+        {
+            const uint32_t p = b + lane, s0 = src_at(p);
+            t = term(p, p < e ? prev[s0] : 0.0);
+        }
+        uint32_t s1 = src_at(b + 32 + lane);
         for (uint32_t base = b; base < e; base += 32) {
-            const uint32_t p = base + lane;
-            const bool ok = p < e;
-            const double t = ok ? __dmul_rn(w ? w[p] : 1.0, prev[other[p]]) : 0.0;
-            s = fold_lanes_in_order(s, t, __ballot_sync(0xffffffffu, ok));
+            const uint32_t p = base + lane, p1 = p + 32;
+            const double pr1 = p1 < e ? prev[s1] : 0.0;
+            const uint32_t s2 = src_at(base + 64 + lane);
+            s = fold_lanes_in_order(s, t, __ballot_sync(0xffffffffu, p < e));
+            t = term(p1, pr1);
+            s1 = s2;
         }
         if (lane == 0) {
             next[i] = s;
