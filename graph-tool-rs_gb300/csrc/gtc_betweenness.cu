@@ -16,15 +16,19 @@
 //   sigma    each new vertex pulls its path count from the in-edges whose
 //            source lies one level up (each parallel edge is a distinct
 //            shortest path, as in the reference's non_tree_edge)
-//   back     levels deepest first: each vertex v sums
-//            (sigma_v / sigma_t)(1 + dep_t) over its out-edges into the next
-//            level, adds each term to its edge and the sum to v
+//   back     levels deepest first: each vertex v sums sigma_v * c_t over its
+//            out-edges into the next level, c_t = (1 + dep_t) / sigma_t
+//            formed once per vertex when its dependency is final, adds each
+//            term to its edge and the sum to v
 // The order a level is discovered in does not enter any sum: every sum is a
 // pull over one vertex's edges in storage order, lane-strided and merged by
 // a fixed shuffle tree (over the pair, or over the warp for a vertex with
-// more than 32 edges), so the result is deterministic.  It differs from the reference's
-// only by the association of FP64 sums (the reference accumulates in BFS
-// dequeue order), which is why parity is stated as a tolerance, as the
+// more than 32 edges), so the result is deterministic.  It differs from the
+// reference's by the association of FP64 sums (the reference accumulates in
+// BFS dequeue order) and in the last bits of each term (the reference forms
+// (sigma_v / sigma_t)(1 + dep_t) per edge: one divide per edge, where an
+// FP64 divide is a dozen FP64 instructions on a GPU whose FP64 pipe is the
+// back phase's bound), which is why parity is stated as a tolerance, as the
 // reference's own tests state it against their independent Brandes
 // (crates/gt-algo/tests/u16_centrality.rs:707-760).  Path counts are sums of
 // integers, exact while they stay below 2^53.
@@ -32,9 +36,9 @@
 // Each CTA keeps its own partial vertex and edge maps; they are folded in
 // CTA order at the end (the reference folds per-chunk partials in chunk
 // order, centrality.rs:669-679).  Scratch per CTA: distance, path count,
-// dependency, the BFS order, the set-aside list and level offsets (40 bytes
-// per vertex with the partial vertex map) plus 8 bytes per edge; G is cut to
-// fit a memory budget.
+// factor c, the BFS order, the set-aside list and level offsets (40 bytes per
+// vertex with the partial vertex map) plus 8 bytes per edge; G is cut to fit
+// a memory budget.
 #include <algorithm>
 #include <vector>
 
@@ -64,7 +68,7 @@ struct BcArgs {
     // per CTA c: [c * n] slices (lvl: [c * (n + 2)], ebp: [c * m])
     int* dist;
     double* sigma;
-    double* dep;
+    double* coef;  // (1 + dependency) / path count, once the dependency is final
     uint32_t* order;
     uint32_t* lvl;
     uint32_t* heavy;  // the vertices of the current phase set aside for whole warps
@@ -128,7 +132,7 @@ __global__ void __launch_bounds__(BC_NT) k_bc(BcArgs A) {
     const size_t c = blockIdx.x;
     int* dist = A.dist + c * A.n;
     double* sigma = A.sigma + c * A.n;
-    double* dep = A.dep + c * A.n;
+    double* coef = A.coef + c * A.n;
     uint32_t* order = A.order + c * A.n;
     uint32_t* lvl = A.lvl + c * ((size_t)A.n + 2);
     uint32_t* heavy = A.heavy + c * A.n;
@@ -208,6 +212,11 @@ __global__ void __launch_bounds__(BC_NT) k_bc(BcArgs A) {
             ++L;
         }
         // L levels are non-empty (0 .. L-1); the deepest has no dependency
+        for (uint32_t i = lvl[L - 1] + threadIdx.x; i < lvl[L]; i += BC_NT) {
+            const uint32_t v = order[i];
+            coef[v] = __ddiv_rn(1.0, sigma[v]);
+        }
+        __syncthreads();
         for (int lev = (int)L - 2; lev >= 0; --lev) {
             phase(lvl[lev], lvl[lev + 1], false,
                   [&](uint32_t v, uint32_t l, uint32_t S) {
@@ -215,25 +224,23 @@ __global__ void __launch_bounds__(BC_NT) k_bc(BcArgs A) {
                       double acc = 0.0;
                       walk_out(A, v, l, S, [&](uint32_t t, uint32_t e) {
                           if (t == v || dist[t] != lev + 1) return;
-                          const double f =
-                              __dmul_rn(__ddiv_rn(sv, sigma[t]), __dadd_rn(1.0, dep[t]));
+                          const double f = __dmul_rn(sv, coef[t]);
                           acc = __dadd_rn(acc, f);
                           ebp[e] = __dadd_rn(ebp[e], f);  // one term per edge and source
                       });
                       return acc;
                   },
                   [&](uint32_t v, double acc) {
-                      dep[v] = acc;
+                      coef[v] = __ddiv_rn(__dadd_rn(1.0, acc), sigma[v]);
                       if (v != s) vbp[v] = __dadd_rn(vbp[v], acc);
                   });
         }
-        // clear what this source touched
+        // clear what this source touched (coef is written before it is read)
         const uint32_t tot = lvl[L];
         for (uint32_t i = threadIdx.x; i < tot; i += BC_NT) {
             const uint32_t v = order[i];
             dist[v] = -1;
             sigma[v] = 0.0;
-            dep[v] = 0.0;
         }
         __syncthreads();
     }
@@ -297,12 +304,11 @@ void betweenness(gtc_graph* g, const gtc_view* vw, bool undirected, double* vb_h
                                      std::max<uint32_t>(nsrc, 1u), budget / per_cta});
     G = std::max<uint64_t>(G, 1);
     DevBuf<int> dist(G * n, s);
-    DevBuf<double> sigma(G * n, s), dep(G * n, s), vbp(G * n, s), ebp(G * m, s);
+    DevBuf<double> sigma(G * n, s), coef(G * n, s), vbp(G * n, s), ebp(G * m, s);
     DevBuf<uint32_t> order(G * n, s), heavy(G * n, s), lvl(G * ((uint64_t)n + 2), s);
     if (n) {
         GTC_CUDA(cudaMemsetAsync(dist.get(), 0xFF, G * n * sizeof(int), s));
         GTC_CUDA(cudaMemsetAsync(sigma.get(), 0, G * n * sizeof(double), s));
-        GTC_CUDA(cudaMemsetAsync(dep.get(), 0, G * n * sizeof(double), s));
         GTC_CUDA(cudaMemsetAsync(vbp.get(), 0, G * n * sizeof(double), s));
     }
     if (m) GTC_CUDA(cudaMemsetAsync(ebp.get(), 0, G * m * sizeof(double), s));
@@ -315,7 +321,7 @@ void betweenness(gtc_graph* g, const gtc_view* vw, bool undirected, double* vb_h
         A.push_off = view.push_off, A.push_other = view.push_other, A.push_eid = view.push_eid;
         A.pull_off = view.pull_off, A.pull_other = view.pull_other, A.pull_eid = view.pull_eid;
         A.undirected = undirected ? 1 : 0;
-        A.dist = dist.get(), A.sigma = sigma.get(), A.dep = dep.get();
+        A.dist = dist.get(), A.sigma = sigma.get(), A.coef = coef.get();
         A.order = order.get(), A.lvl = lvl.get(), A.heavy = heavy.get();
         A.vbp = vbp.get(), A.ebp = ebp.get();
         A.m = m;
