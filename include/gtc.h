@@ -36,6 +36,12 @@
  *   - "Host" pointers are ordinary CPU memory; they may be pageable or
  *     pinned.  Calls are synchronous with respect to host buffers.
  *   - A handle is not thread-safe; use one handle per thread or lock.
+ *   - A handle keeps what its graph alone determines, built by the first
+ *     call that needs it: the FP32 sweep schedules of the plain and reversed
+ *     views, their unweighted degrees, sink flags and FP32 inverse degrees
+ *     (13 bytes per vertex and view), and, for the last weight map an FP32
+ *     call used (same address, type and contents), that map's FP32 layouts
+ *     and weighted degrees.  A filtered view builds its own per call.
  *   - No entry point falls back to the CPU: without a usable CUDA device
  *     they return GTC_ERR_NO_DEVICE.
  */
