@@ -227,9 +227,11 @@ __device__ __forceinline__ void plan_range(uint64_t n, uint64_t chunks, uint64_t
     e = s + base + (k < rem ? 1 : 0);
 }
 
-// One thread per row, the in-edge loop sequential in storage order.
-// Rows of more than F64_SHORT entries are summed by a warp (k_pr_f64_long,
-// k_ev_f64_long); shorter rows by a thread each.
+// Weighted views: one thread per row, the in-edge loop sequential in storage
+// order; rows of more than F64_SHORT entries are summed by a warp
+// (k_pr_f64_long, k_ev_f64_long), whose 32 lanes form 32 terms per divide
+// or multiply instruction.  Unweighted views: a thread per row of any length
+// (k_pr_f64_rows_q, k_ev_f64_rows_u), the terms needing no per-edge FP64 work.
 constexpr uint32_t F64_SHORT = 32;
 
 // FP64 on this GPU: an add has a latency of about 64 cycles, and a warp
