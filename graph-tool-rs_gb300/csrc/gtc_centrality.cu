@@ -269,7 +269,10 @@ __device__ __forceinline__ double fold_seq(double acc, uint64_t b, uint64_t e, I
 #pragma unroll
         for (int j = 0; j < FU; ++j) t[FD][j] = p + FD * FU + j < e ? val(sn[j]) : 0.0;
 #pragma unroll
-        for (int j = 0; j < FU; ++j) sn[j] = p + (FD + 1) * FU + j < e ? idx(p + (FD + 1) * FU + j) : 0u;
+        for (int j = 0; j < FU; ++j) {
+            const uint64_t q = p + (FD + 1) * FU + j;
+            sn[j] = q < e ? idx(q) : 0u;
+        }
 #pragma unroll
         for (int j = 0; j < FU; ++j)
             if (p + j < e) acc = __dadd_rn(acc, t[0][j]);
